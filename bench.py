@@ -1,0 +1,422 @@
+#!/usr/bin/env python
+"""Benchmark of the classic unsplit 2D step on GB300.
+
+Headline workload: shallow water, Roe solver with entropy fix, 2048x2048 on
+[-2.5,2.5]^2, radial dam break (h=2 for r<0.5 else 1), wall boundaries, MC
+limiter, transverse_waves=2, CFL 0.9.  One bench step is one time step of
+that grid; --steps K times K of them (default 1000, the full run).
+
+Metric: Gcell-updates/s (interior cells x accepted steps / time).
+  value    plain FP64 step, device-timed with CUDA events around each step
+           kernel; the L2 is flushed (256 MB write) before every timed step.
+  e2e      the per-step path of the reference with host buffers: every step
+           copies the state from pinned host memory, runs the step and copies
+           the new state and the Courant number back (gclaw_step_host).
+  roofline the dominant kernel (the step) against HBM bandwidth: algorithmic
+           bytes 2*m*8 = 48 B per cell-update; an FP64-pipe roofline is given
+           beside it because the FP64 step is bound by the FP64 units.
+  cpu_baseline the CPU oracle (C restatement of the Fortran step) on the host
+           cores, OpenMP over all of them, on a bounded sample of steps.
+  fp32_bulk  the FP32-bulk variant (FP32 fluxes, FP64 state and CFL) on the
+           same K steps, with its relative L1 error against the FP64 result.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+Under torchrun with N ranks each rank advances its own replica (the path
+has no exchange step), timing is the max over ranks and value is the
+aggregate over all ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("Gcell-updates/s on 1 GB300: plain FP64 vs FP32/batched at stated error; "
+          "%HBM peak")
+UNIT = "Gcell-updates/s"
+FALLBACK_HBM_GBS = 6800.0
+FALLBACK_BF16_TFLOPS = 1900.0
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--mx", type=int, default=2048)
+    p.add_argument("--e2e-steps", type=int, default=50)
+    p.add_argument("--no-variants", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ plumbing
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def init_dist(world, backend):
+    import torch.distributed as dist
+
+    if world > 1 and not dist.is_initialized():
+        dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(x, world, device):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        try:
+            d = json.load(open(path))
+            hbm = d.get("hbm_gbs") or d.get("hbm_GBs")
+            return float(hbm), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic(kernel_tag):
+    """DRAM bytes per cell-update from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_cell_update:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------ GPU timing
+def timed_steps(dev, steps, flush, torch):
+    """Time `steps` controlled step launches, one CUDA-event pair around each
+    launch, flushing L2 before each.  Returns (seconds, accepted steps)."""
+    stream = torch.cuda.current_stream()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    c0 = dev.read_ctrl()
+    for k in range(steps):
+        flush.fill_(k & 0xff)
+        starts[k].record(stream)
+        dev.advance(1)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    c1 = dev.read_ctrl()
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    return ms * 1e-3, c1.numsteps - c0.numsteps, c1
+
+
+def run_variant(w, precision, steps, warmup, torch, flush, world, device):
+    from clawpack_gb300.device import DeviceProblem
+
+    dev = DeviceProblem(w.solver_struct(precision), device=device)
+    dev.upload(w.q0)
+    dev.ctrl_init(0.0, w.dt_initial, math.inf, cfl_max=w.cfl_max, cfl_desired=w.cfl_desired,
+                  max_accepted=-1, max_steps=10 ** 9)
+    dev.advance(warmup)
+    torch.cuda.synchronize()
+    barrier(world)
+    secs, accepted, c = timed_steps(dev, steps, flush, torch)
+    barrier(world)
+    secs = max_over_ranks(secs, world, device)
+    return secs, accepted, c, dev
+
+
+def e2e_host_steps(w, nsteps, torch, device):
+    """Per-step host-buffer path through gclaw_step_host (pinned buffers),
+    with PyClaw's host-side dt control.  Returns (seconds, accepted, bytes)."""
+    from clawpack_gb300 import _lib
+
+    s = w.solver_struct(0)
+    L = _lib.lib()
+    nb = L.gclaw_step_workspace_bytes(ctypes.byref(s))
+    ws = torch.empty(nb + 256, dtype=torch.uint8, device=device)
+    base = (ws.data_ptr() + 255) // 256 * 256
+    qb = w.q0.nbytes
+    h = [torch.empty(qb, dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+    np.frombuffer(h[0].numpy(), dtype=np.float64)[:] = np.asfortranarray(w.q0).ravel(order="F")
+    cfl = ctypes.c_double()
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    dt = w.dt_initial
+    src, accepted = 0, 0
+    # one untimed call to load the module and set kernel attributes
+    rc = L.gclaw_step_host(ctypes.byref(s), ctypes.c_void_p(h[0].data_ptr()),
+                           ctypes.c_void_p(h[1].data_ptr()), dt, ctypes.c_void_p(base), nb,
+                           ctypes.byref(cfl), sp)
+    _lib.check(rc, "gclaw_step_host")
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(nsteps):
+        rc = L.gclaw_step_host(ctypes.byref(s), ctypes.c_void_p(h[src].data_ptr()),
+                               ctypes.c_void_p(h[1 - src].data_ptr()), dt,
+                               ctypes.c_void_p(base), nb, ctypes.byref(cfl), sp)
+        _lib.check(rc, "gclaw_step_host")
+        if cfl.value <= w.cfl_max:
+            accepted += 1
+            src ^= 1
+        dt = min(1e99, dt * w.cfl_desired / cfl.value)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    return max(e0.elapsed_time(e1) * 1e-3, wall), accepted, qb
+
+
+def cpu_baseline(w, target_s=15.0):
+    """The CPU oracle on the host cores (OpenMP, all threads) over a bounded
+    number of full-grid steps."""
+    from oracle import ref
+
+    threads = os.cpu_count() or 1
+    ref.lib()
+    q = w.q0
+    dt = w.dt_initial
+
+    def one(q, dt):
+        return ref.step(w.rp_id, w.pd_array(), q, w.dx, w.dy, dt, w.bc_lower, w.bc_upper,
+                        w.order, w.transverse_waves, w.mthlim(), nthreads=threads)
+
+    t0 = time.perf_counter()
+    q, cfl, _ = one(q, dt)
+    first = time.perf_counter() - t0
+    n = int(max(1, min(20, target_s / max(first, 1e-3))))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        dt = dt * w.cfl_desired / cfl
+        q, cfl, _ = one(q, dt)
+    secs = time.perf_counter() - t0
+    cells = w.mx * w.my
+    return {"value": cells * n / secs * 1e-9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n} full {w.mx}x{w.my} steps of the same problem on {threads} threads "
+                      f"(OpenMP over slices), {secs:.1f} s"}
+
+
+# ------------------------------------------------------------------ arms
+def run_ours(args):
+    import torch
+
+    world, rank, local = dist_env()
+    device = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(device)
+    init_dist(world, "nccl")
+    from clawpack_gb300 import workloads
+
+    w = workloads.shallow_dam_break(args.mx, args.mx, nsteps=args.warmup + args.steps)
+    m = w.num_eqn
+    cells = w.mx * w.my
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=device)
+    peak, peak_kind = measured_peaks()
+
+    clocks = ClockSampler(local).start()
+    secs, accepted, c64, dev64 = run_variant(w, 0, args.steps, args.warmup, torch, flush, world,
+                                             device)
+    clk = clocks.stop()
+    value = world * cells * accepted / secs * 1e-9
+    t_kernel = secs / args.steps
+    alg_bytes = 2 * m * 8 * cells
+    achieved = alg_bytes / t_kernel * 1e-9
+    traffic_per_cell = profiled_traffic("step_fp64_shallow")
+    out = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(secs / args.steps * 1e3, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"shallow_dam_break {w.mx}x{w.my} Roe+efix, wall BCs, MC, "
+                               "transverse_waves=2, CFL 0.9, FP64",
+                   "mx": w.mx, "my": w.my, "accepted_steps": accepted,
+                   "l2": "flushed before every timed step (256 MB write, untimed)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_source": f"{peak_kind} HBM copy bandwidth",
+                     "traffic": (None if traffic_per_cell is None
+                                 else round(traffic_per_cell * cells)),
+                     "alg_bytes_per_launch": alg_bytes,
+                     "note": "the FP64 step is bound by the FP64 pipe, not HBM"},
+        "clocks": clk,
+        "gpu_launches": args.steps,
+    }
+    if not args.no_variants:
+        s32, acc32, c32, dev32 = run_variant(w, 1, args.steps, args.warmup, torch, flush, world,
+                                             device)
+        v32 = world * cells * acc32 / s32 * 1e-9
+        q64 = dev64.q[c64.parity]
+        q32 = dev32.q[c32.parity]
+        err = float((q32 - q64).abs().sum() / q64.abs().sum())
+        a32 = alg_bytes / (s32 / args.steps) * 1e-9
+        out["fp32_bulk"] = {"value": round(v32, 4), "unit": UNIT, "dtype": "f32 fluxes, f64 q",
+                            "rel_l1_vs_fp64": err, "speedup_vs_fp64": round(v32 / value, 3),
+                            "ms_per_step": round(s32 / args.steps * 1e3, 4),
+                            "roofline": {"bound": "hbm", "achieved": round(a32, 1),
+                                         "peak": peak, "unit": "GB/s",
+                                         "frac": round(a32 / peak, 4)}}
+        out["gpu_launches"] += args.steps
+        del dev32
+    # end to end through the C ABI with host buffers, every step
+    e2e_s, e2e_acc, qb = e2e_host_steps(w, args.e2e_steps, torch, device)
+    e2e_s = max_over_ranks(e2e_s, world, device)
+    out["e2e"] = {"value": round(world * cells * e2e_acc / e2e_s * 1e-9, 4), "unit": UNIT,
+                  "h2d_bytes_per_step": qb, "d2h_bytes_per_step": qb + 8 + 4,
+                  "steps": args.e2e_steps,
+                  "path": "gclaw_step_host: pinned host q -> device, fused BC + step, "
+                          "new q and CFL -> host, every step"}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cw = w
+        out["cpu_baseline"] = cpu_baseline(cw)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference arm: the CPU oracle (the reference Fortran step cannot
+    be built here; its restatement is timed instead) on the host cores, each
+    step one time step of a bounded 2048 x 128 band of the same problem."""
+    world, rank, _ = dist_env()
+    if world > 1 and rank != 0:
+        return
+    from clawpack_gb300 import workloads
+    from oracle import ref
+
+    threads = os.cpu_count() or 1
+    band = 128
+    w = workloads.shallow_dam_break(args.mx, args.mx)
+    lo = args.mx // 2 - band // 2
+    q = np.asfortranarray(w.q0[:, :, lo:lo + band])
+    ref.lib()
+    dt = w.dt_initial
+    cfl = w.cfl_desired
+
+    def one(q, dt):
+        return ref.step(w.rp_id, w.pd_array(), q, w.dx, w.dy, dt, w.bc_lower, w.bc_upper,
+                        w.order, w.transverse_waves, w.mthlim(), nthreads=threads)
+
+    for _ in range(args.warmup):
+        q, cfl, _ = one(q, dt)
+        dt = dt * w.cfl_desired / cfl
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        q, cfl, _ = one(q, dt)
+        dt = dt * w.cfl_desired / cfl
+    secs = time.perf_counter() - t0
+    cells = args.mx * band
+    v = cells * args.steps / secs * 1e-9
+    sample = (f"each step: one time step of a {args.mx}x{band} band through the dam "
+              f"(same dx, dt rule, BCs), CPU oracle on {threads} threads")
+    out = {"impl": "reference", "metric": METRIC, "value": round(v, 5), "unit": UNIT,
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(secs / args.steps * 1e3, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"shallow_dam_break {args.mx}x{args.mx} band sample",
+                      "band_rows": band},
+           "cpu_baseline": {"value": round(v, 5), "unit": UNIT, "cores": threads,
+                            "kind": "port", "sample": sample},
+           "e2e": {"value": round(v, 5), "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,396 @@
+// gclaw_riemann.cuh -- device Riemann solvers and wave limiters for the
+// classic unsplit 2D step.
+//
+// Normal solvers (rpn2) and transverse solvers (rpt2) of the clawpack.riemann
+// modules acoustics_2D, shallow_roe_with_efix_2D and euler_4wave_2D
+// (upstream riemann/src/rpn2_acoustics.f90, rpt2_acoustics.f90,
+// rpn2_shallow_roe_with_efix.f90, rpt2_shallow_roe_with_efix.f90,
+// rpn2_euler_4wave.f90, rpt2_euler.f90; the riemann submodule is empty in the
+// mounted clawpack 5.14.0 tree, meson.build:65).  The mathematics is that of
+// LeVeque, Finite Volume Methods for Hyperbolic Problems (2002): Roe
+// linearisations (sec. 15.3), the Harten-Hyman entropy fix (sec. 15.3.5),
+// transverse splitting with the transverse eigenstructure at the edge's Roe
+// state (ch. 21), wave limiters (sec. 6.12).
+//
+// Every expression is written in the operation order of the CPU oracle so
+// that an FP64 build without multiply-add contraction reproduces it bit for
+// bit.  Differences from the reference's per-edge code are layout only: the
+// Roe state of an edge is computed once by rpn2 and handed to rpt2 (rpt2
+// recomputes the identical expressions upstream), and ixy is a template
+// parameter.
+//
+// Conventions: ql is the cell left of (below) the edge, qr the cell right of
+// (above) it.  W is [MW][M] row-major, s is [MW].  mu = IXY is the normal
+// momentum/velocity component, mv = 3 - IXY the transverse one.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+namespace gclaw {
+
+template <typename T>
+__device__ __forceinline__ T tmin(T a, T b) { return fmin(a, b); }
+template <typename T>
+__device__ __forceinline__ T tmax(T a, T b) { return fmax(a, b); }
+template <>
+__device__ __forceinline__ float tmin<float>(float a, float b) { return fminf(a, b); }
+template <>
+__device__ __forceinline__ float tmax<float>(float a, float b) { return fmaxf(a, b); }
+
+// ---------------------------------------------------------------------------
+// Constant-coefficient acoustics: q = (p, u, v); speeds -c, +c.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct RpAcoustics {
+    static constexpr int M = 3, MW = 2, NR = 0;
+    struct Params {
+        T cc, zz;
+    };
+    static Params make(const double *pd) { return Params{(T)pd[2], (T)pd[3]}; }
+
+    template <int IXY>
+    __device__ __forceinline__ static bool rpn2(const Params &P, const T *ql, const T *qr, T *W,
+                                                T *s, T *am, T *ap, T *R) {
+        constexpr int mu = IXY, mv = 3 - IXY;
+        T d0 = qr[0] - ql[0];
+        T d1 = qr[mu] - ql[mu];
+        T a1 = (-d0 + P.zz * d1) / ((T)2 * P.zz);
+        T a2 = (d0 + P.zz * d1) / ((T)2 * P.zz);
+        W[0] = -a1 * P.zz; W[mu] = a1; W[mv] = (T)0;
+        s[0] = -P.cc;
+        W[3] = a2 * P.zz; W[3 + mu] = a2; W[3 + mv] = (T)0;
+        s[1] = P.cc;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            am[k] = s[0] * W[k];
+            ap[k] = s[1] * W[3 + k];
+        }
+        return false;
+    }
+
+    template <int IXY>
+    __device__ __forceinline__ static void rpt2(const Params &P, const T *R, const T *asdq, T *bm,
+                                                T *bp) {
+        constexpr int mu = IXY, mv = 3 - IXY;
+        T a1 = (-asdq[0] + P.zz * asdq[mv]) / ((T)2 * P.zz);
+        T a2 = (asdq[0] + P.zz * asdq[mv]) / ((T)2 * P.zz);
+        bm[0] = P.cc * a1 * P.zz; bm[mu] = (T)0; bm[mv] = -P.cc * a1;
+        bp[0] = P.cc * a2 * P.zz; bp[mu] = (T)0; bp[mv] = P.cc * a2;
+    }
+};
+
+// Sum of min(sb,0) Wb and max(sb,0) Wb over the transverse waves.
+template <typename T, int M, int MW>
+__device__ __forceinline__ void split_sum(const T *sb, const T *wb, T *bm, T *bp) {
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        T lo = (T)0, hi = (T)0;
+#pragma unroll
+        for (int p = 0; p < MW; p++) {
+            lo = lo + tmin(sb[p], (T)0) * wb[M * p + k];
+            hi = hi + tmax(sb[p], (T)0) * wb[M * p + k];
+        }
+        bm[k] = lo;
+        bp[k] = hi;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Shallow water, Roe solver with Harten-Hyman entropy fix: q = (h, hu, hv).
+// Roe state kept for rpt2: R = (ubar, vbar, cbar).
+// ---------------------------------------------------------------------------
+template <typename T>
+struct RpShallow {
+    static constexpr int M = 3, MW = 3, NR = 3;
+    struct Params {
+        T g;
+        double gd;
+    };
+    static Params make(const double *pd) { return Params{(T)pd[0], pd[0]}; }
+
+    // Roe averages.  In FP32 bulk mode, depths below 1e-3 take the square
+    // roots and quotients in FP64 (near-dry states).
+    __device__ __forceinline__ static void roe(const Params &P, T hl, T hr, T hul, T hur, T hvl,
+                                               T hvr, T &u, T &v, T &c) {
+        if (sizeof(T) == 4 && (hl < (T)1e-3 || hr < (T)1e-3)) {
+            double sl = sqrt((double)hl), sr = sqrt((double)hr), s2 = sl + sr;
+            u = (T)(((double)hul / sl + (double)hur / sr) / s2);
+            v = (T)(((double)hvl / sl + (double)hvr / sr) / s2);
+            c = (T)sqrt(P.gd * (((double)hl + (double)hr) * 0.5));
+            return;
+        }
+        T hsqrtl = sqrt(hl), hsqrtr = sqrt(hr);
+        T hsq2 = hsqrtl + hsqrtr;
+        u = (hul / hsqrtl + hur / hsqrtr) / hsq2;
+        v = (hvl / hsqrtl + hvr / hsqrtr) / hsq2;
+        T hbar = (hl + hr) * (T)0.5;
+        c = sqrt(P.g * hbar);
+    }
+
+    template <int IXY>
+    __device__ __forceinline__ static bool rpn2(const Params &P, const T *ql, const T *qr, T *W,
+                                                T *s, T *am, T *ap, T *R) {
+        constexpr int mu = IXY, mv = 3 - IXY;
+        const T g = P.g;
+        T hl = ql[0], hr = qr[0];
+        T ubar, vbar, cbar;
+        roe(P, hl, hr, ql[mu], qr[mu], ql[mv], qr[mv], ubar, vbar, cbar);
+        R[0] = ubar; R[1] = vbar; R[2] = cbar;
+        T d0 = hr - hl, d1 = qr[mu] - ql[mu], d2 = qr[mv] - ql[mv];
+        T a1 = ((ubar + cbar) * d0 - d1) * ((T)0.5 / cbar);
+        T a2 = -vbar * d0 + d2;
+        T a3 = (-(ubar - cbar) * d0 + d1) * ((T)0.5 / cbar);
+        T *w1 = W, *w2 = W + 3, *w3 = W + 6;
+        w1[0] = a1; w1[mu] = a1 * (ubar - cbar); w1[mv] = a1 * vbar;
+        s[0] = ubar - cbar;
+        w2[0] = (T)0; w2[mu] = (T)0; w2[mv] = a2;
+        s[1] = ubar;
+        w3[0] = a3; w3[mu] = a3 * (ubar + cbar); w3[mv] = a3 * vbar;
+        s[2] = ubar + cbar;
+
+        // entropy fix: amdq first, apdq = sum(s W) - amdq
+        T s0 = ql[mu] / hl - sqrt(g * hl);
+        if (s0 >= (T)0 && s[0] > (T)0) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) am[k] = (T)0;
+        } else {
+            T h1 = hl + w1[0];
+            T hu1 = ql[mu] + w1[mu];
+            T s1 = hu1 / h1 - sqrt(g * h1);
+            T sfract;
+            if (s0 < (T)0 && s1 > (T)0)
+                sfract = s0 * (s1 - s[0]) / (s1 - s0);
+            else if (s[0] < (T)0)
+                sfract = s[0];
+            else
+                sfract = (T)0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) am[k] = sfract * w1[k];
+            if (s[1] < (T)0) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) am[k] = am[k] + s[1] * w2[k];
+                T s03 = qr[mu] / hr + sqrt(g * hr);
+                T h3 = hr - w3[0];
+                T hu3 = qr[mu] - w3[mu];
+                T s3 = hu3 / h3 + sqrt(g * h3);
+                bool add = true;
+                if (s3 < (T)0 && s03 > (T)0)
+                    sfract = s3 * (s03 - s[2]) / (s03 - s3);
+                else if (s[2] < (T)0)
+                    sfract = s[2];
+                else
+                    add = false;
+                if (add) {
+#pragma unroll
+                    for (int k = 0; k < 3; k++) am[k] = am[k] + sfract * w3[k];
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            T df = (T)0;
+#pragma unroll
+            for (int p = 0; p < 3; p++) df = df + s[p] * W[3 * p + k];
+            ap[k] = df - am[k];
+        }
+        return false;
+    }
+
+    template <int IXY>
+    __device__ __forceinline__ static void rpt2(const Params &P, const T *R, const T *asdq, T *bm,
+                                                T *bp) {
+        constexpr int mu = IXY, mv = 3 - IXY;
+        T ubar = R[0], vbar = R[1], cbar = R[2];
+        T a1 = ((vbar + cbar) * asdq[0] - asdq[mv]) * ((T)0.5 / cbar);
+        T a2 = asdq[mu] - ubar * asdq[0];
+        T a3 = (-(vbar - cbar) * asdq[0] + asdq[mv]) * ((T)0.5 / cbar);
+        T wb[9], sb[3];
+        wb[0] = a1; wb[mu] = a1 * ubar; wb[mv] = a1 * (vbar - cbar);
+        sb[0] = vbar - cbar;
+        wb[3] = (T)0; wb[3 + mu] = a2; wb[3 + mv] = (T)0;
+        sb[1] = vbar;
+        wb[6] = a3; wb[6 + mu] = a3 * ubar; wb[6 + mv] = a3 * (vbar + cbar);
+        sb[2] = vbar + cbar;
+        split_sum<T, 3, 3>(sb, wb, bm, bp);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// 2D Euler, Roe solver with 4 waves (acoustic u-c, entropy u, shear u,
+// acoustic u+c) and optional Harten-Hyman entropy fix: q = (rho, rhou, rhov, E).
+// Roe state kept for rpt2: R = (u, v, enth, u2v2, a, g1a2, euv).
+// ---------------------------------------------------------------------------
+template <typename T>
+struct RpEuler {
+    static constexpr int M = 4, MW = 4, NR = 7;
+    struct Params {
+        T gamma, gamma1;
+        int efix;
+    };
+    static Params make(const double *pd) {
+        return Params{(T)pd[0], (T)(pd[0] - 1.0), pd[1] != 0.0 ? 1 : 0};
+    }
+
+    __device__ __forceinline__ static T pressure(T gamma1, const T *q) {
+        return gamma1 * (q[3] - (T)0.5 * (q[1] * q[1] + q[2] * q[2]) / q[0]);
+    }
+
+    template <int IXY>
+    __device__ __forceinline__ static bool rpn2(const Params &P, const T *ql, const T *qr, T *W,
+                                                T *s, T *am, T *ap, T *R) {
+        constexpr int mu = IXY, mv = 3 - IXY;
+        const T gamma = P.gamma, gamma1 = P.gamma1;
+        T pl = pressure(gamma1, ql);
+        T pr = pressure(gamma1, qr);
+        T u, v, enth;
+        if (sizeof(T) == 4 && (ql[0] < (T)1e-3 || qr[0] < (T)1e-3)) {
+            // near-vacuum states: Roe averages in FP64
+            double rl = sqrt((double)ql[0]), rr = sqrt((double)qr[0]), rs = rl + rr;
+            u = (T)(((double)ql[mu] / rl + (double)qr[mu] / rr) / rs);
+            v = (T)(((double)ql[mv] / rl + (double)qr[mv] / rr) / rs);
+            enth = (T)((((double)ql[3] + (double)pl) / rl + ((double)qr[3] + (double)pr) / rr) / rs);
+        } else {
+            T rhsqrtl = sqrt(ql[0]), rhsqrtr = sqrt(qr[0]);
+            T rhsq2 = rhsqrtl + rhsqrtr;
+            u = (ql[mu] / rhsqrtl + qr[mu] / rhsqrtr) / rhsq2;
+            v = (ql[mv] / rhsqrtl + qr[mv] / rhsqrtr) / rhsq2;
+            enth = ((ql[3] + pl) / rhsqrtl + (qr[3] + pr) / rhsqrtr) / rhsq2;
+        }
+        T u2v2 = u * u + v * v;
+        T c2 = gamma1 * (enth - (T)0.5 * u2v2);
+        bool bad = !(c2 > (T)0);
+        T a = sqrt(c2);
+        T g1a2 = gamma1 / c2;
+        T euv = enth - u2v2;
+        R[0] = u; R[1] = v; R[2] = enth; R[3] = u2v2; R[4] = a; R[5] = g1a2; R[6] = euv;
+        T d0 = qr[0] - ql[0], dmu = qr[mu] - ql[mu], dmv = qr[mv] - ql[mv], d3 = qr[3] - ql[3];
+        T a3 = g1a2 * (euv * d0 + u * dmu + v * dmv - d3);
+        T a2 = dmv - v * d0;
+        T a4 = (dmu + (a - u) * d0 - a * a3) / ((T)2 * a);
+        T a1 = d0 - a3 - a4;
+        T *w1 = W, *w2 = W + 4, *w3 = W + 8, *w4 = W + 12;
+        w1[0] = a1; w1[mu] = a1 * (u - a); w1[mv] = a1 * v; w1[3] = a1 * (enth - u * a);
+        s[0] = u - a;
+        w2[0] = a3; w2[mu] = a3 * u; w2[mv] = a3 * v; w2[3] = a3 * (T)0.5 * u2v2;
+        s[1] = u;
+        w3[0] = (T)0; w3[mu] = (T)0; w3[mv] = a2; w3[3] = a2 * v;
+        s[2] = u;
+        w4[0] = a4; w4[mu] = a4 * (u + a); w4[mv] = a4 * v; w4[3] = a4 * (enth + u * a);
+        s[3] = u + a;
+
+        if (!P.efix) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                am[k] = (T)0;
+                ap[k] = (T)0;
+            }
+#pragma unroll
+            for (int p = 0; p < 4; p++) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (s[p] < (T)0)
+                        am[k] = am[k] + s[p] * W[4 * p + k];
+                    else
+                        ap[k] = ap[k] + s[p] * W[4 * p + k];
+                }
+            }
+            return bad;
+        }
+        T cim1 = sqrt(gamma * pl / ql[0]);
+        T s0 = ql[mu] / ql[0] - cim1;
+        if (s0 >= (T)0 && s[0] > (T)0) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) am[k] = (T)0;
+        } else {
+            T rho1 = ql[0] + w1[0];
+            T rhou1 = ql[mu] + w1[mu];
+            T rhov1 = ql[mv] + w1[mv];
+            T en1 = ql[3] + w1[3];
+            T p1 = gamma1 * (en1 - (T)0.5 * (rhou1 * rhou1 + rhov1 * rhov1) / rho1);
+            T c1 = sqrt(gamma * p1 / rho1);
+            T s1 = rhou1 / rho1 - c1;
+            T sfract;
+            if (s0 < (T)0 && s1 > (T)0)
+                sfract = s0 * (s1 - s[0]) / (s1 - s0);
+            else if (s[0] < (T)0)
+                sfract = s[0];
+            else
+                sfract = (T)0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) am[k] = sfract * w1[k];
+            if (s[1] < (T)0) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) am[k] = am[k] + s[1] * w2[k];
+#pragma unroll
+                for (int k = 0; k < 4; k++) am[k] = am[k] + s[2] * w3[k];
+                T ci = sqrt(gamma * pr / qr[0]);
+                T s3 = qr[mu] / qr[0] + ci;
+                T rho2 = qr[0] - w4[0];
+                T rhou2 = qr[mu] - w4[mu];
+                T rhov2 = qr[mv] - w4[mv];
+                T en2 = qr[3] - w4[3];
+                T p2 = gamma1 * (en2 - (T)0.5 * (rhou2 * rhou2 + rhov2 * rhov2) / rho2);
+                T cc2 = sqrt(gamma * p2 / rho2);
+                T s2 = rhou2 / rho2 + cc2;
+                bool add = true;
+                if (s2 < (T)0 && s3 > (T)0)
+                    sfract = s2 * (s3 - s[3]) / (s3 - s2);
+                else if (s[3] < (T)0)
+                    sfract = s[3];
+                else
+                    add = false;
+                if (add) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) am[k] = am[k] + sfract * w4[k];
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            T df = (T)0;
+#pragma unroll
+            for (int p = 0; p < 4; p++) df = df + s[p] * W[4 * p + k];
+            ap[k] = df - am[k];
+        }
+        return bad;
+    }
+
+    template <int IXY>
+    __device__ __forceinline__ static void rpt2(const Params &P, const T *R, const T *asdq, T *bm,
+                                                T *bp) {
+        constexpr int mu = IXY, mv = 3 - IXY;
+        T u = R[0], v = R[1], enth = R[2], u2v2 = R[3], a = R[4], g1a2 = R[5], euv = R[6];
+        T a3 = g1a2 * (euv * asdq[0] + u * asdq[mu] + v * asdq[mv] - asdq[3]);
+        T a2 = asdq[mu] - u * asdq[0];
+        T a4 = (asdq[mv] + (a - v) * asdq[0] - a * a3) / ((T)2 * a);
+        T a1 = asdq[0] - a3 - a4;
+        T wb[16], sb[4];
+        wb[0] = a1; wb[mu] = a1 * u; wb[mv] = a1 * (v - a); wb[3] = a1 * (enth - v * a);
+        sb[0] = v - a;
+        wb[4] = a3; wb[4 + mu] = a3 * u; wb[4 + mv] = a3 * v; wb[7] = a3 * (T)0.5 * u2v2;
+        sb[1] = v;
+        wb[8] = (T)0; wb[8 + mu] = a2; wb[8 + mv] = (T)0; wb[11] = a2 * u;
+        sb[2] = v;
+        wb[12] = a4; wb[12 + mu] = a4 * u; wb[12 + mv] = a4 * (v + a); wb[15] = a4 * (enth + v * a);
+        sb[3] = v + a;
+        split_sum<T, 4, 4>(sb, wb, bm, bp);
+    }
+};
+
+// Wave limiter phi(theta): 1 minmod, 2 superbee, 3 van Leer, 4 MC.
+template <typename T>
+__device__ __forceinline__ T philim(int id, T r) {
+    switch (id) {
+    case 1: return tmax((T)0, tmin((T)1, r));
+    case 2: return tmax((T)0, tmax(tmin((T)1, (T)2 * r), tmin((T)2, r)));
+    case 3: return (r + fabs(r)) / ((T)1 + fabs(r));
+    case 4: {
+        T c = ((T)1 + r) / (T)2;
+        return tmax((T)0, tmin(c, tmin((T)2, (T)2 * r)));
+    }
+    default: return (T)1;
+    }
+}
+
+}  // namespace gclaw

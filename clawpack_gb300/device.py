@@ -1,0 +1,118 @@
+"""Device-resident problem state for libgclaw.so: two FP64 state buffers, a
+gclaw_ctrl block, and thin wrappers over the C ABI.
+
+PyTorch provides device memory and the stream; every kernel is libgclaw's.
+The state buffers hold q as PyClaw lays it out, (num_eqn, mx, my) in Fortran
+order, which is a C-contiguous torch tensor of shape (my, mx, num_eqn).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def _stream_handle(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def make_solver_struct(rp_id, mx, my, dx, dy, bc_lower, bc_upper, mthlim, order, tw,
+                       precision, problem_data):
+    s = _lib.GclawSolver()
+    s.rp = int(rp_id)
+    s.mx, s.my = int(mx), int(my)
+    s.dx, s.dy = float(dx), float(dy)
+    for d in range(2):
+        s.bc_lower[d] = int(bc_lower[d])
+        s.bc_upper[d] = int(bc_upper[d])
+    lim = list(mthlim) + [0] * (_lib.MAX_WAVES - len(mthlim))
+    for p in range(_lib.MAX_WAVES):
+        s.mthlim[p] = int(lim[p])
+    s.order = int(order)
+    s.transverse_waves = int(tw)
+    s.precision = int(precision)
+    pd = list(problem_data) + [0.0] * (8 - len(problem_data))
+    for i in range(8):
+        s.problem_data[i] = float(pd[i])
+    return s
+
+
+class DeviceProblem:
+    """Two state buffers + control block on one CUDA device."""
+
+    def __init__(self, solver_struct, device=None, strict=False):
+        self.s = solver_struct
+        self.L = L = _lib.lib(strict)
+        _lib.check(L.gclaw_check(ctypes.byref(self.s)), "gclaw_check")
+        m = ctypes.c_int()
+        mw = ctypes.c_int()
+        _lib.check(L.gclaw_rp_shape(self.s.rp, ctypes.byref(m), ctypes.byref(mw)))
+        self.m, self.mw = m.value, mw.value
+        self.mx, self.my = self.s.mx, self.s.my
+        self.device = torch.device(device or "cuda")
+        shape = (self.my, self.mx, self.m)
+        self.q = [torch.empty(shape, dtype=torch.float64, device=self.device),
+                  torch.empty(shape, dtype=torch.float64, device=self.device)]
+        self.ctrl = torch.zeros(256, dtype=torch.uint8, device=self.device)
+        self._ctrl_host = torch.empty(256, dtype=torch.uint8, pin_memory=True)
+        self.ctrl_init(0.0, 1.0, 0.0)
+
+    # -- host <-> device ---------------------------------------------------
+    def upload(self, q, buf=0):
+        """Copy a host (num_eqn, mx, my) array into state buffer ``buf``."""
+        qf = np.asfortranarray(q, dtype=np.float64)
+        if qf.shape != (self.m, self.mx, self.my):
+            raise ValueError(f"q has shape {qf.shape}, expected {(self.m, self.mx, self.my)}")
+        self.q[buf].copy_(torch.from_numpy(qf.T))
+
+    def download(self, buf=0):
+        """State buffer ``buf`` as a host (num_eqn, mx, my) Fortran-ordered array."""
+        return np.asfortranarray(self.q[buf].cpu().numpy().T)
+
+    # -- control block -------------------------------------------------------
+    def ctrl_init(self, t, dt, t_end, cfl_max=1.0, cfl_desired=0.9, dt_max=1e99,
+                  max_steps=10000, max_accepted=-1, dt_variable=True, stream=None):
+        _lib.check(self.L.gclaw_ctrl_init(
+            ctypes.c_void_p(self.ctrl.data_ptr()), float(t), float(dt), float(t_end),
+            float(cfl_max), float(cfl_desired), float(dt_max), int(max_steps),
+            int(max_accepted), 1 if dt_variable else 0, _stream_handle(stream)), "gclaw_ctrl_init")
+
+    def read_ctrl(self, stream=None):
+        """Synchronise the stream and return a host copy of the gclaw_ctrl."""
+        self._ctrl_host.copy_(self.ctrl, non_blocking=True)
+        (stream or torch.cuda.current_stream()).synchronize()
+        c = _lib.GclawCtrl()
+        ctypes.memmove(ctypes.addressof(c), self._ctrl_host.data_ptr(), _lib.CTRL_BYTES)
+        return c
+
+    # -- stepping ------------------------------------------------------------
+    def advance(self, nlaunch, stream=None):
+        """Enqueue ``nlaunch`` controlled steps (no synchronisation)."""
+        _lib.check(self.L.gclaw_advance(
+            ctypes.byref(self.s), ctypes.c_void_p(self.q[0].data_ptr()),
+            ctypes.c_void_p(self.q[1].data_ptr()), ctypes.c_void_p(self.ctrl.data_ptr()),
+            int(nlaunch), _stream_handle(stream)), "gclaw_advance")
+
+    def step(self, dt, src=0, stream=None):
+        """One step with explicit dt from buffer ``src`` into ``1 - src``; the
+        Courant number is left in the control block (see ``read_ctrl``)."""
+        _lib.check(self.L.gclaw_step(
+            ctypes.byref(self.s), ctypes.c_void_p(self.q[src].data_ptr()),
+            ctypes.c_void_p(self.q[1 - src].data_ptr()), float(dt),
+            ctypes.c_void_p(self.ctrl.data_ptr()), _stream_handle(stream)), "gclaw_step")
+
+    def evolve(self, t, dt, t_end, *, cfl_max=1.0, cfl_desired=0.9, dt_max=1e99,
+               max_steps=10000, max_accepted=-1, dt_variable=True, batch=32, stream=None):
+        """Device-controlled evolve of buffer 0 (already uploaded); returns the
+        final control block.  The accepted state is in buffer ``ctrl.parity``."""
+        self.ctrl_init(t, dt, t_end, cfl_max, cfl_desired, dt_max, max_steps, max_accepted,
+                       dt_variable, stream)
+        while True:
+            self.advance(batch, stream)
+            c = self.read_ctrl(stream)
+            if c.done:
+                return c

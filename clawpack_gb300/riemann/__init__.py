@@ -1,0 +1,28 @@
+"""Riemann-solver descriptors named like the clawpack.riemann modules.
+
+PyClaw passes a solver module to ``ClawSolver2D(riemann.<name>)`` and reads its
+shape from ``riemann.static`` (upstream riemann/riemann/static.py; the
+riemann submodule is empty in the mounted clawpack 5.14.0 tree,
+meson.build:65).  Here each name is a small descriptor object carrying the
+same ``__name__``, ``num_eqn`` and ``num_waves`` plus the id of the device
+solver in libgclaw.so.
+"""
+from __future__ import annotations
+
+from types import SimpleNamespace
+
+from .. import _lib
+from . import static
+
+
+def _descriptor(name, rp_id):
+    return SimpleNamespace(__name__=f"clawpack_gb300.riemann.{name}", name=name, rp_id=rp_id,
+                           num_eqn=static.num_eqn[name], num_waves=static.num_waves[name])
+
+
+acoustics_2D = _descriptor("acoustics_2D", _lib.RP_ACOUSTICS_2D)
+shallow_roe_with_efix_2D = _descriptor("shallow_roe_with_efix_2D",
+                                       _lib.RP_SHALLOW_ROE_WITH_EFIX_2D)
+euler_4wave_2D = _descriptor("euler_4wave_2D", _lib.RP_EULER_4WAVE_2D)
+
+__all__ = ["acoustics_2D", "shallow_roe_with_efix_2D", "euler_4wave_2D", "static"]

@@ -1,0 +1,11 @@
+"""Shapes of the supported Riemann solvers, as in clawpack.riemann.static."""
+num_eqn = {
+    "acoustics_2D": 3,
+    "shallow_roe_with_efix_2D": 3,
+    "euler_4wave_2D": 4,
+}
+num_waves = {
+    "acoustics_2D": 2,
+    "shallow_roe_with_efix_2D": 3,
+    "euler_4wave_2D": 4,
+}

@@ -1,0 +1,197 @@
+"""Initial and boundary data of the benchmark problems.
+
+Each function returns a ``Workload`` describing one problem of the classic
+2D path: solver, problem data, grid, boundary conditions, limiters, CFL
+targets, the initial state q0 (num_eqn, mx, my) in Fortran order, and either
+an end time or a number of accepted steps.  All data are synthetic and
+seeded; no dataset is involved.
+
+  acoustics_radial   2D acoustics, 200x200 on [-1,1]^2, rho=1, K=4 (c=2),
+                     p = exp(-100 r^2), u=v=0, extrapolation BCs, MC limiter,
+                     transverse_waves=2, CFL 0.9, t_final 0.6, 10 frames
+  shallow_dam_break  shallow water Roe + entropy fix, 2048x2048 on
+                     [-2.5,2.5]^2, g=1, h=2 for r<0.5 else 1, wall BCs, MC,
+                     transverse_waves=2, CFL 0.9, 1000 steps
+  euler_quadrants    2D Euler Roe 4-wave, gamma=1.4, 4096x4096 on [0,1]^2,
+                     four quadrant states drawn from a seed (rho, p in
+                     U[0.1,1.5], u, v in U[-1,1]), extrapolation BCs,
+                     superbee, CFL 0.8, 500 steps
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .pyclaw.limiters import tvd
+from .pyclaw.solver import BC
+
+EULER_SEED = 20261204
+
+
+@dataclass
+class Workload:
+    name: str
+    rp_name: str
+    rp_id: int
+    problem_data: dict
+    lower: tuple
+    upper: tuple
+    mx: int
+    my: int
+    q0: np.ndarray
+    bc_lower: list
+    bc_upper: list
+    limiters: int
+    order: int = 2
+    transverse_waves: int = 2
+    cfl_desired: float = 0.9
+    cfl_max: float = 1.0
+    dt_initial: float = 0.1
+    tfinal: float = None
+    nsteps: int = None
+    num_output_times: int = 10
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def dx(self):
+        return (self.upper[0] - self.lower[0]) / self.mx
+
+    @property
+    def dy(self):
+        return (self.upper[1] - self.lower[1]) / self.my
+
+    @property
+    def num_eqn(self):
+        return self.q0.shape[0]
+
+    def pd_array(self):
+        """problem_data in the gclaw_solver.problem_data layout."""
+        pd = self.problem_data
+        if self.rp_id == _lib.RP_ACOUSTICS_2D:
+            return [pd["rho"], pd["bulk"], pd["cc"], pd["zz"]]
+        if self.rp_id == _lib.RP_SHALLOW_ROE_WITH_EFIX_2D:
+            return [pd["grav"]]
+        return [pd["gamma"], 1.0 if pd.get("efix", True) else 0.0]
+
+    @property
+    def num_waves(self):
+        return {_lib.RP_ACOUSTICS_2D: 2, _lib.RP_SHALLOW_ROE_WITH_EFIX_2D: 3,
+                _lib.RP_EULER_4WAVE_2D: 4}[self.rp_id]
+
+    def mthlim(self, num_waves=None):
+        return [self.limiters] * (num_waves or self.num_waves)
+
+    def solver_struct(self, precision=_lib.PREC_FP64):
+        """The gclaw_solver C struct of this workload."""
+        from .device import make_solver_struct
+
+        return make_solver_struct(self.rp_id, self.mx, self.my, self.dx, self.dy,
+                                  self.bc_lower, self.bc_upper, self.mthlim(), self.order,
+                                  self.transverse_waves, precision, self.pd_array())
+
+
+def _centers(lower, upper, n):
+    d = (upper - lower) / n
+    return lower + (np.arange(n) + 0.5) * d
+
+
+def acoustics_radial(mx=200, my=200):
+    x = _centers(-1.0, 1.0, mx)
+    y = _centers(-1.0, 1.0, my)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    rho, bulk = 1.0, 4.0
+    cc = math.sqrt(bulk / rho)
+    zz = rho * cc
+    q = np.zeros((3, mx, my), order="F")
+    q[0] = np.exp(-100.0 * (X * X + Y * Y))
+    return Workload("acoustics_radial", "acoustics_2D", _lib.RP_ACOUSTICS_2D,
+                    dict(rho=rho, bulk=bulk, cc=cc, zz=zz), (-1.0, -1.0), (1.0, 1.0), mx, my, q,
+                    [BC.extrap, BC.extrap], [BC.extrap, BC.extrap], tvd.MC, cfl_desired=0.9,
+                    dt_initial=0.1, tfinal=0.6, num_output_times=10)
+
+
+def shallow_dam_break(mx=2048, my=2048, nsteps=1000):
+    x = _centers(-2.5, 2.5, mx)
+    y = _centers(-2.5, 2.5, my)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    q = np.zeros((3, mx, my), order="F")
+    q[0] = np.where(np.sqrt(X * X + Y * Y) < 0.5, 2.0, 1.0)
+    g = 1.0
+    dx = 5.0 / mx
+    # first dt from the initial wave speed sqrt(g h_max), so no attempt is rejected
+    dt0 = 0.9 * dx / math.sqrt(g * 2.0)
+    return Workload("shallow_dam_break", "shallow_roe_with_efix_2D",
+                    _lib.RP_SHALLOW_ROE_WITH_EFIX_2D, dict(grav=g), (-2.5, -2.5), (2.5, 2.5), mx,
+                    my, q, [BC.wall, BC.wall], [BC.wall, BC.wall], tvd.MC, cfl_desired=0.9,
+                    dt_initial=dt0, nsteps=nsteps)
+
+
+def euler_quadrant_states(seed=EULER_SEED):
+    """Four (rho, u, v, p) states, quadrants ordered (x<.5,y<.5), (x>.5,y<.5),
+    (x<.5,y>.5), (x>.5,y>.5)."""
+    rng = np.random.default_rng(seed)
+    st = []
+    for _ in range(4):
+        rho = rng.uniform(0.1, 1.5)
+        u = rng.uniform(-1.0, 1.0)
+        v = rng.uniform(-1.0, 1.0)
+        p = rng.uniform(0.1, 1.5)
+        st.append((rho, u, v, p))
+    return st
+
+
+def euler_quadrants(mx=4096, my=4096, nsteps=500, seed=EULER_SEED, gamma=1.4):
+    x = _centers(0.0, 1.0, mx)
+    y = _centers(0.0, 1.0, my)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    states = euler_quadrant_states(seed)
+    q = np.zeros((4, mx, my), order="F")
+    quad = (X > 0.5).astype(int) + 2 * (Y > 0.5).astype(int)
+    smax = 0.0
+    for k, (rho, u, v, p) in enumerate(states):
+        msk = quad == k
+        q[0][msk] = rho
+        q[1][msk] = rho * u
+        q[2][msk] = rho * v
+        q[3][msk] = p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)
+        smax = max(smax, max(abs(u), abs(v)) + math.sqrt(gamma * p / rho))
+    dt0 = 0.8 * min(1.0 / mx, 1.0 / my) / smax
+    return Workload("euler_quadrants", "euler_4wave_2D", _lib.RP_EULER_4WAVE_2D,
+                    dict(gamma=gamma, efix=True), (0.0, 0.0), (1.0, 1.0), mx, my, q,
+                    [BC.extrap, BC.extrap], [BC.extrap, BC.extrap], tvd.superbee,
+                    cfl_desired=0.8, dt_initial=dt0, nsteps=nsteps,
+                    meta=dict(seed=seed, states=states))
+
+
+def make_claw(w: Workload, precision="fp64"):
+    """A pyclaw Controller set up for workload ``w``."""
+    from . import riemann
+    from .pyclaw import ClawSolver2D, Controller, Dimension, Domain, Solution, State
+
+    solver = ClawSolver2D(getattr(riemann, w.rp_name))
+    solver.dimensional_split = False
+    solver.transverse_waves = w.transverse_waves
+    solver.order = w.order
+    solver.limiters = w.limiters
+    solver.cfl_desired = w.cfl_desired
+    solver.cfl_max = w.cfl_max
+    solver.dt_initial = w.dt_initial
+    solver.bc_lower = list(w.bc_lower)
+    solver.bc_upper = list(w.bc_upper)
+    solver.precision = precision
+    x = Dimension(w.lower[0], w.upper[0], w.mx, name="x")
+    y = Dimension(w.lower[1], w.upper[1], w.my, name="y")
+    domain = Domain([x, y])
+    state = State(domain, solver.num_eqn)
+    state.problem_data.update(w.problem_data)
+    state.q = w.q0
+    claw = Controller()
+    claw.solution = Solution(state, domain)
+    claw.solver = solver
+    if w.tfinal is not None:
+        claw.tfinal = w.tfinal
+        claw.num_output_times = w.num_output_times
+    return claw

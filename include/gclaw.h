@@ -1,0 +1,193 @@
+/*
+ * gclaw.h -- C ABI of libgclaw.so, the GB300 (sm_103a) classic unsplit 2D
+ * wave-propagation step.
+ *
+ * The reference path this replaces is PyClaw's ClawSolver2D.step() calling
+ * the f2py module classic2.step2(...) with the rpn2/rpt2 callbacks of a
+ * clawpack.riemann module (upstream pyclaw/src/pyclaw/classic/solver.py and
+ * step2.f90; the submodules are empty in the mounted umbrella tree,
+ * .gitmodules:1-21, and are mapped by meson.build:62-76).  The f2py array
+ * convention is kept: q is (num_eqn, mx, my) in Fortran order, i.e. the
+ * component index varies fastest, then x, then y.  With ghost cells it is
+ * PyClaw's qbc, (num_eqn, mx+4, my+4) for num_ghost = 2.
+ *
+ * Conventions
+ *   - Every pointer named *_dev is device memory owned by the caller; the
+ *     library allocates nothing and only borrows pointers.
+ *   - stream is a cudaStream_t passed as void* (NULL = legacy stream).
+ *   - Return value: 0 = GCLAW_OK, < 0 argument / CUDA errors, > 0 numerical
+ *     conditions (non-physical state, CFL rejection with fixed dt, step cap).
+ *   - One gclaw_ctrl per concurrently advancing problem; calls that share a
+ *     gclaw_ctrl must be ordered on one stream.
+ */
+#ifndef GCLAW_H
+#define GCLAW_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Riemann solvers: the clawpack.riemann modules of the same name
+ * (conda-recipe/meta.yaml:36 imports clawpack.riemann.euler_4wave_2D). */
+#define GCLAW_RP_ACOUSTICS_2D 1             /* m=3 (p,u,v), 2 waves; pd: rho, bulk, cc, zz */
+#define GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D 2 /* m=3 (h,hu,hv), 3 waves; pd: grav */
+#define GCLAW_RP_EULER_4WAVE_2D 3           /* m=4 (rho,rhou,rhov,E), 4 waves; pd: gamma, efix */
+
+/* Boundary conditions: the values of pyclaw.BC. */
+#define GCLAW_BC_CUSTOM 0 /* not supported: rejected with GCLAW_ERR_UNSUPPORTED */
+#define GCLAW_BC_EXTRAP 1
+#define GCLAW_BC_PERIODIC 2
+#define GCLAW_BC_WALL 3
+
+/* Wave limiters: the values of pyclaw.limiters.tvd. */
+#define GCLAW_LIM_NONE 0
+#define GCLAW_LIM_MINMOD 1
+#define GCLAW_LIM_SUPERBEE 2
+#define GCLAW_LIM_VANLEER 3
+#define GCLAW_LIM_MC 4
+
+/* Arithmetic of the flux computation.  Storage of q is FP64 in both. */
+#define GCLAW_PREC_FP64 0      /* plain FP64, the drop-in for the Fortran step */
+#define GCLAW_PREC_FP32_BULK 1 /* FP32 waves/fluxes, FP64 accumulation and CFL */
+
+/* Status codes. */
+#define GCLAW_OK 0
+#define GCLAW_ERR_ARG (-1)
+#define GCLAW_ERR_CUDA (-2)
+#define GCLAW_ERR_UNSUPPORTED (-4)
+#define GCLAW_ERR_WORKSPACE (-5)
+#define GCLAW_NONPHYSICAL 2  /* NaN Courant number or negative Euler c^2 */
+#define GCLAW_CFL_FIXED_DT 3 /* step rejected while dt_variable = 0 */
+#define GCLAW_MAX_STEPS 4    /* attempts reached max_steps before tend */
+
+#define GCLAW_MAX_WAVES 4
+
+/* Solver description: the attributes of pyclaw.ClawSolver2D that the step
+ * reads, plus the grid.  mx, my >= 2; num_ghost is fixed at 2. */
+typedef struct gclaw_solver {
+    int rp;                       /* GCLAW_RP_* */
+    int mx, my;                   /* interior cells */
+    double dx, dy;                /* cell sizes */
+    int bc_lower[2], bc_upper[2]; /* GCLAW_BC_* for x and y */
+    int mthlim[GCLAW_MAX_WAVES];  /* limiter per wave family (solver.limiters) */
+    int order;                    /* 1 or 2 (solver.order) */
+    int transverse_waves;         /* 0, 1 or 2 (solver.transverse_waves) */
+    int precision;                /* GCLAW_PREC_* */
+    double problem_data[8];       /* state.problem_data, layout per GCLAW_RP_* */
+} gclaw_solver;
+
+/* Time-step control block, resident in device memory.  The step kernel's
+ * last block applies PyClaw's evolve_to_time rules to it (upstream
+ * pyclaw/src/pyclaw/solver.py): reject when cfl > cfl_max, otherwise
+ * t += dt; then dt = min(dt_max, dt*cfl_desired/cfl), clipped to land on
+ * t_end.  Fields marked (in) are set by the caller before advancing. */
+typedef struct gclaw_ctrl {
+    double t;            /* time of the accepted state (in/out) */
+    double dt;           /* dt of the next attempt (in/out) */
+    double t_start;      /* time at the start of this evolve call (in) */
+    double t_end;        /* stop when t >= t_end (in) */
+    double cfl_max;      /* (in) */
+    double cfl_desired;  /* (in) */
+    double dt_max;       /* (in) */
+    double cfl;          /* Courant number of the last attempt (out) */
+    double cflmax;       /* largest accepted Courant number (out) */
+    double dtmin, dtmax; /* range of dt chosen (out) */
+    unsigned long long smax_bits[2]; /* scratch: max |s| of x and y edges */
+    int parity;          /* buffer holding the accepted state, 0 or 1 (in/out) */
+    int numsteps;        /* accepted steps (out) */
+    int attempts;        /* attempted steps (out) */
+    int max_steps;       /* cap on attempts, PyClaw's solver.max_steps (in) */
+    int max_accepted;    /* stop after this many accepted steps; < 0: none (in) */
+    int dt_variable;     /* 1 (default) or 0 (in) */
+    int done;            /* 1 once finished or failed (out) */
+    int status;          /* GCLAW_OK or a positive status (out) */
+    unsigned int blocks_done; /* scratch: last-block counter */
+    unsigned int flags;       /* scratch: non-physical flag of this attempt */
+} gclaw_ctrl;
+
+/* Library version string. */
+const char *gclaw_version(void);
+
+/* Text for a status code. */
+const char *gclaw_strerror(int status);
+
+/* Number of equations and waves of a Riemann solver id (0 on success). */
+int gclaw_rp_shape(int rp, int *num_eqn, int *num_waves);
+
+/* Validate a solver description (0 if it can be stepped). */
+int gclaw_check(const gclaw_solver *s);
+
+/* Set a control block to its initial state on stream: t, dt, t_end, the
+ * PyClaw controls, parity 0, counters zero.  max_accepted < 0 disables the
+ * step-count stop; dt is clipped to t_end as PyClaw does before a step.
+ * The fields are written by a one-thread kernel enqueued on stream, so the
+ * call neither copies from host memory nor synchronises, and can be
+ * captured in a CUDA graph. */
+int gclaw_ctrl_init(gclaw_ctrl *ctrl_dev, double t, double dt, double t_end, double cfl_max,
+                    double cfl_desired, double dt_max, int max_steps, int max_accepted,
+                    int dt_variable, void *stream);
+
+/* Drop-in for classic2.step2 (upstream pyclaw/src/pyclaw/classic/step2.f90):
+ * one unsplit step of a ghost-filled qbc.  qold_dev and qnew_dev are
+ * (num_eqn, mx+4, my+4) Fortran order; the interior of qnew_dev receives the
+ * updated state (its ghost entries are left untouched).  ws_dev is a
+ * gclaw_ctrl used as reduction scratch (its smax_bits/blocks_done/flags must
+ * be zero before the first call, which gclaw_ctrl_init ensures; each call
+ * leaves them zero).  The Courant number is written to *cfl_out after the
+ * stream is synchronised.  Returns GCLAW_NONPHYSICAL if a Riemann problem
+ * met a non-physical state. */
+int gclaw_step2(const gclaw_solver *s, const double *qold_dev, double *qnew_dev, double dt,
+                gclaw_ctrl *ws_dev, double *cfl_out, void *stream);
+
+/* Fused step with on-device boundary conditions: reads q_dev
+ * (num_eqn, mx, my), applies solver.bc_lower/bc_upper as PyClaw's
+ * _apply_bcs would, writes qnew_dev, and leaves the Courant number in
+ * ws_dev->cfl (no synchronisation).  Replaces the pair
+ * ClawSolver2D._apply_bcs + classic2.step2. */
+int gclaw_step(const gclaw_solver *s, const double *q_dev, double *qnew_dev, double dt,
+               gclaw_ctrl *ws_dev, void *stream);
+
+/* Enqueue nlaunch controlled steps on stream without synchronising: each
+ * reads dt and parity from ctrl_dev, steps q{parity} into q{1-parity}, and
+ * its last block applies the evolve_to_time rules.  Steps after ctrl->done
+ * is set return at once.  The launches can be captured in a CUDA graph. */
+int gclaw_advance(const gclaw_solver *s, double *q0_dev, double *q1_dev, gclaw_ctrl *ctrl_dev,
+                  int nlaunch, void *stream);
+
+/* Device bytes gclaw_step_host needs in ws_dev. */
+size_t gclaw_step_workspace_bytes(const gclaw_solver *s);
+
+/* One step from host memory: the per-step path of the reference, where
+ * ClawSolver2D.step() hands numpy arrays to classic2.step2 every step
+ * (upstream pyclaw/src/pyclaw/classic/solver.py), here replacing
+ * _apply_bcs + step2.  Copies q_host (num_eqn, mx, my) to the device, runs
+ * gclaw_step, copies the new state to qnew_host and the Courant number to
+ * *cfl_out, then synchronises the stream.  ws_dev (caller-owned, 256-byte
+ * aligned, at least gclaw_step_workspace_bytes) holds the control block and
+ * both device states. */
+int gclaw_step_host(const gclaw_solver *s, const double *q_host, double *qnew_host, double dt,
+                    void *ws_dev, size_t ws_bytes, double *cfl_out, void *stream);
+
+/* Device bytes gclaw_evolve_host needs in ws_dev. */
+size_t gclaw_evolve_workspace_bytes(const gclaw_solver *s);
+
+/* End-to-end run from host memory, the analogue of PyClaw's
+ * solver.evolve_to_time: copies q_host (num_eqn, mx, my) to the device,
+ * advances from t to t_end (or for max_accepted accepted steps when
+ * max_accepted >= 0) with the evolve_to_time rules on the device, and copies
+ * the accepted state back to q_out_host.  ws_dev (caller-owned, at least
+ * gclaw_evolve_workspace_bytes) holds the two state buffers and the control
+ * block; *ctrl_out receives the final control block.  Launches steps in
+ * batches of `batch` (<= 0: 32) between checks of ctrl->done. */
+int gclaw_evolve_host(const gclaw_solver *s, const double *q_host, double *q_out_host, double t,
+                      double dt, double t_end, int max_accepted, double cfl_max,
+                      double cfl_desired, double dt_max, int max_steps, void *ws_dev,
+                      size_t ws_bytes, int batch, gclaw_ctrl *ctrl_out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GCLAW_H */

@@ -1,0 +1,769 @@
+/*
+ * classic2_ref.c -- CPU oracle for the PyClaw classic unsplit 2D step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: only tests/,
+ * __graft_entry__.smoke() and the CPU-baseline leg of bench.py may load it.
+ * The product path (clawpack_gb300) never links or calls it.
+ *
+ * PARITY UNPINNED.  The reference (clawpack 5.14.0, umbrella repository)
+ * declares the code of this path in git submodules that are empty in the
+ * mounted tree (.gitmodules:1-21; meson.build:62-76 maps 'pyclaw' to
+ * pyclaw/src and 'riemann' to riemann).  The files this oracle follows are the
+ * upstream ones, absent here:
+ *     pyclaw/src/pyclaw/classic/step2.f90     (step2: the unsplit 2D step)
+ *     pyclaw/src/pyclaw/classic/flux2.f90     (flux2: one 1D slice)
+ *     pyclaw/src/pyclaw/classic/limiter.f90   (wave limiter + philim)
+ *     pyclaw/src/pyclaw/solver.py             (_apply_bcs ghost fill)
+ *     riemann/src/rpn2_acoustics.f90,  rpt2_acoustics.f90
+ *     riemann/src/rpn2_shallow_roe_with_efix.f90, rpt2_shallow_roe_with_efix.f90
+ *     riemann/src/rpn2_euler_4wave.f90, rpt2_euler.f90
+ * It is a restatement, in original code, of the published method that the
+ * reference names as its algorithm source (CITATION.md:19-41):
+ * R. J. LeVeque, J. Comput. Phys. 131 (1997) 327-353, and LeVeque, "Finite
+ * Volume Methods for Hyperbolic Problems" (2002), ch. 6 (limiters), ch. 15
+ * (Roe solvers, Harten-Hyman entropy fix), ch. 19-21 (unsplit 2D method with
+ * transverse propagation of fluctuations and of correction waves).
+ *
+ * Floating-point order.  Every accumulation is written in the order the
+ * serial Fortran step performs it (slice by slice, x-sweep then y-sweep,
+ * each qnew(i,j) receiving the row j-1, j, j+1 terms of the x-sweep and then
+ * the column i-1, i, i+1 terms of the y-sweep).  Build with
+ * -ffp-contract=off so that no multiply-add is fused.  The slices are
+ * independent, so they run in parallel (OpenMP) with per-slice outputs and a
+ * separate ordered accumulation pass; the arithmetic per cell is unchanged.
+ *
+ * Memory layout: q with ghost cells is PyClaw's qbc, shape
+ * (num_eqn, mx+2g, my+2g) in Fortran order, i.e. the component index varies
+ * fastest, then x, then y.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define RP_ACOUSTICS 1
+#define RP_SHALLOW_ROE_EFIX 2
+#define RP_EULER_4WAVE 3
+
+#define BC_CUSTOM 0
+#define BC_EXTRAP 1
+#define BC_PERIODIC 2
+#define BC_WALL 3
+
+#define MAXM 4
+#define MAXW 4
+
+#define ERR_ARG -1
+#define ERR_ALLOC -3
+#define ERR_NONPHYSICAL 2
+
+typedef struct {
+    int id, m, mw;
+    double pd[8];
+} rp_t;
+
+static int rp_shape(int id, int *m, int *mw)
+{
+    switch (id) {
+    case RP_ACOUSTICS: *m = 3; *mw = 2; return 0;
+    case RP_SHALLOW_ROE_EFIX: *m = 3; *mw = 3; return 0;
+    case RP_EULER_4WAVE: *m = 4; *mw = 4; return 0;
+    default: return ERR_ARG;
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Normal Riemann solvers.  ql = state of the cell left of the edge (cell e-1),
+ * qr = state of the cell right of it (cell e).  ixy = 1 for an x-edge,
+ * 2 for a y-edge; mu is the normal momentum/velocity component, mv the
+ * transverse one.  wave is [mw][m], s is [mw].
+ * Returns nonzero for a non-physical state (negative Euler sound speed
+ * squared), which upstream stops on.
+ * ---------------------------------------------------------------------- */
+
+/* Constant-coefficient acoustics, q = (p, u, v); eigenvalues -c, +c with
+ * eigenvectors (-Z, 1, 0) and (Z, 1, 0) in (p, normal u, transverse u),
+ * Z = rho c (upstream rpn2_acoustics.f90). */
+static int rpn2_acoustics(const rp_t *rp, int ixy, const double *ql, const double *qr,
+                          double *wave, double *s, double *amdq, double *apdq)
+{
+    const double cc = rp->pd[2], zz = rp->pd[3];
+    const int mu = ixy, mv = 3 - ixy;
+    double d0 = qr[0] - ql[0];
+    double d1 = qr[mu] - ql[mu];
+    double a1 = (-d0 + zz * d1) / (2.0 * zz);
+    double a2 = (d0 + zz * d1) / (2.0 * zz);
+    double *w1 = wave, *w2 = wave + 3;
+    w1[0] = -a1 * zz; w1[mu] = a1; w1[mv] = 0.0;
+    s[0] = -cc;
+    w2[0] = a2 * zz; w2[mu] = a2; w2[mv] = 0.0;
+    s[1] = cc;
+    for (int k = 0; k < 3; k++) {
+        amdq[k] = s[0] * w1[k];
+        apdq[k] = s[1] * w2[k];
+    }
+    return 0;
+}
+
+/* Shallow water Roe solver, q = (h, hu, hv), with the Harten-Hyman entropy
+ * fix for transonic rarefactions (FVMHP sec. 15.3.5; upstream
+ * rpn2_shallow_roe_with_efix.f90). */
+static int rpn2_shallow(const rp_t *rp, int ixy, const double *ql, const double *qr,
+                        double *wave, double *s, double *amdq, double *apdq)
+{
+    const double g = rp->pd[0];
+    const int mu = ixy, mv = 3 - ixy;
+    double hl = ql[0], hr = qr[0];
+    double hsqrtl = sqrt(hl), hsqrtr = sqrt(hr);
+    double hsq2 = hsqrtl + hsqrtr;
+    double ubar = (ql[mu] / hsqrtl + qr[mu] / hsqrtr) / hsq2;
+    double vbar = (ql[mv] / hsqrtl + qr[mv] / hsqrtr) / hsq2;
+    double hbar = (hl + hr) * 0.5;
+    double cbar = sqrt(g * hbar);
+    double d0 = hr - hl, d1 = qr[mu] - ql[mu], d2 = qr[mv] - ql[mv];
+    double a1 = ((ubar + cbar) * d0 - d1) * (0.5 / cbar);
+    double a2 = -vbar * d0 + d2;
+    double a3 = (-(ubar - cbar) * d0 + d1) * (0.5 / cbar);
+    double *w1 = wave, *w2 = wave + 3, *w3 = wave + 6;
+    w1[0] = a1; w1[mu] = a1 * (ubar - cbar); w1[mv] = a1 * vbar;
+    s[0] = ubar - cbar;
+    w2[0] = 0.0; w2[mu] = 0.0; w2[mv] = a2;
+    s[1] = ubar;
+    w3[0] = a3; w3[mu] = a3 * (ubar + cbar); w3[mv] = a3 * vbar;
+    s[2] = ubar + cbar;
+
+    /* entropy fix: left-going part amdq, then apdq = (sum s W) - amdq */
+    double sfract;
+    int k;
+    double s0 = ql[mu] / hl - sqrt(g * hl);          /* u - c left of the 1-wave */
+    if (s0 >= 0.0 && s[0] > 0.0) {
+        for (k = 0; k < 3; k++) amdq[k] = 0.0;       /* fully right-going */
+        goto done;
+    }
+    {
+        double h1 = hl + w1[0];
+        double hu1 = ql[mu] + w1[mu];
+        double s1 = hu1 / h1 - sqrt(g * h1);         /* u - c right of the 1-wave */
+        if (s0 < 0.0 && s1 > 0.0)
+            sfract = s0 * (s1 - s[0]) / (s1 - s0);   /* transonic 1-rarefaction */
+        else if (s[0] < 0.0)
+            sfract = s[0];
+        else
+            sfract = 0.0;
+    }
+    for (k = 0; k < 3; k++) amdq[k] = sfract * w1[k];
+    if (s[1] >= 0.0) goto done;
+    for (k = 0; k < 3; k++) amdq[k] = amdq[k] + s[1] * w2[k];
+    {
+        double s03 = qr[mu] / hr + sqrt(g * hr);     /* u + c right of the 3-wave */
+        double h3 = hr - w3[0];
+        double hu3 = qr[mu] - w3[mu];
+        double s3 = hu3 / h3 + sqrt(g * h3);         /* u + c left of the 3-wave */
+        if (s3 < 0.0 && s03 > 0.0)
+            sfract = s3 * (s03 - s[2]) / (s03 - s3); /* transonic 3-rarefaction */
+        else if (s[2] < 0.0)
+            sfract = s[2];
+        else
+            goto done;
+    }
+    for (k = 0; k < 3; k++) amdq[k] = amdq[k] + sfract * w3[k];
+done:
+    for (k = 0; k < 3; k++) {
+        double df = 0.0;
+        for (int p = 0; p < 3; p++) df = df + s[p] * wave[3 * p + k];
+        apdq[k] = df - amdq[k];
+    }
+    return 0;
+}
+
+static double euler_pressure(double gamma1, const double *q)
+{
+    return gamma1 * (q[3] - 0.5 * (q[1] * q[1] + q[2] * q[2]) / q[0]);
+}
+
+/* 2D Euler Roe solver with 4 waves: acoustic (u-c), entropy (u), shear (u),
+ * acoustic (u+c); q = (rho, rho u, rho v, E); optional Harten-Hyman entropy
+ * fix (pd[1] != 0).  Upstream rpn2_euler_4wave.f90. */
+static int rpn2_euler(const rp_t *rp, int ixy, const double *ql, const double *qr,
+                      double *wave, double *s, double *amdq, double *apdq)
+{
+    const double gamma = rp->pd[0], gamma1 = gamma - 1.0;
+    const int efix = rp->pd[1] != 0.0;
+    const int mu = ixy, mv = 3 - ixy;
+    double rhsqrtl = sqrt(ql[0]), rhsqrtr = sqrt(qr[0]);
+    double pl = euler_pressure(gamma1, ql);
+    double pr = euler_pressure(gamma1, qr);
+    double rhsq2 = rhsqrtl + rhsqrtr;
+    double u = (ql[mu] / rhsqrtl + qr[mu] / rhsqrtr) / rhsq2;
+    double v = (ql[mv] / rhsqrtl + qr[mv] / rhsqrtr) / rhsq2;
+    double enth = ((ql[3] + pl) / rhsqrtl + (qr[3] + pr) / rhsqrtr) / rhsq2;
+    double u2v2 = u * u + v * v;
+    double c2 = gamma1 * (enth - 0.5 * u2v2);
+    int bad = !(c2 > 0.0);
+    double a = sqrt(c2);
+    double g1a2 = gamma1 / c2;
+    double euv = enth - u2v2;
+    double d0 = qr[0] - ql[0], dmu = qr[mu] - ql[mu], dmv = qr[mv] - ql[mv], d3 = qr[3] - ql[3];
+    double a3 = g1a2 * (euv * d0 + u * dmu + v * dmv - d3);
+    double a2 = dmv - v * d0;
+    double a4 = (dmu + (a - u) * d0 - a * a3) / (2.0 * a);
+    double a1 = d0 - a3 - a4;
+    double *w1 = wave, *w2 = wave + 4, *w3 = wave + 8, *w4 = wave + 12;
+    w1[0] = a1; w1[mu] = a1 * (u - a); w1[mv] = a1 * v; w1[3] = a1 * (enth - u * a);
+    s[0] = u - a;
+    w2[0] = a3; w2[mu] = a3 * u; w2[mv] = a3 * v; w2[3] = a3 * 0.5 * u2v2;
+    s[1] = u;
+    w3[0] = 0.0; w3[mu] = 0.0; w3[mv] = a2; w3[3] = a2 * v;
+    s[2] = u;
+    w4[0] = a4; w4[mu] = a4 * (u + a); w4[mv] = a4 * v; w4[3] = a4 * (enth + u * a);
+    s[3] = u + a;
+
+    int k, p;
+    if (!efix) {
+        for (k = 0; k < 4; k++) {
+            amdq[k] = 0.0;
+            apdq[k] = 0.0;
+        }
+        for (p = 0; p < 4; p++) {
+            for (k = 0; k < 4; k++) {
+                if (s[p] < 0.0)
+                    amdq[k] = amdq[k] + s[p] * wave[4 * p + k];
+                else
+                    apdq[k] = apdq[k] + s[p] * wave[4 * p + k];
+            }
+        }
+        return bad;
+    }
+    double sfract;
+    {
+        double cim1 = sqrt(gamma * pl / ql[0]);
+        double s0 = ql[mu] / ql[0] - cim1;           /* u - c left of the 1-wave */
+        if (s0 >= 0.0 && s[0] > 0.0) {
+            for (k = 0; k < 4; k++) amdq[k] = 0.0;
+            goto done;
+        }
+        double rho1 = ql[0] + w1[0];
+        double rhou1 = ql[mu] + w1[mu];
+        double rhov1 = ql[mv] + w1[mv];
+        double en1 = ql[3] + w1[3];
+        double p1 = gamma1 * (en1 - 0.5 * (rhou1 * rhou1 + rhov1 * rhov1) / rho1);
+        double c1 = sqrt(gamma * p1 / rho1);
+        double s1 = rhou1 / rho1 - c1;               /* u - c right of the 1-wave */
+        if (s0 < 0.0 && s1 > 0.0)
+            sfract = s0 * (s1 - s[0]) / (s1 - s0);
+        else if (s[0] < 0.0)
+            sfract = s[0];
+        else
+            sfract = 0.0;
+    }
+    for (k = 0; k < 4; k++) amdq[k] = sfract * w1[k];
+    if (s[1] >= 0.0) goto done;
+    for (k = 0; k < 4; k++) amdq[k] = amdq[k] + s[1] * w2[k];
+    for (k = 0; k < 4; k++) amdq[k] = amdq[k] + s[2] * w3[k];
+    {
+        double ci = sqrt(gamma * pr / qr[0]);
+        double s3 = qr[mu] / qr[0] + ci;             /* u + c right of the 4-wave */
+        double rho2 = qr[0] - w4[0];
+        double rhou2 = qr[mu] - w4[mu];
+        double rhov2 = qr[mv] - w4[mv];
+        double en2 = qr[3] - w4[3];
+        double p2 = gamma1 * (en2 - 0.5 * (rhou2 * rhou2 + rhov2 * rhov2) / rho2);
+        double cc2 = sqrt(gamma * p2 / rho2);
+        double s2 = rhou2 / rho2 + cc2;              /* u + c left of the 4-wave */
+        if (s2 < 0.0 && s3 > 0.0)
+            sfract = s2 * (s3 - s[3]) / (s3 - s2);
+        else if (s[3] < 0.0)
+            sfract = s[3];
+        else
+            goto done;
+    }
+    for (k = 0; k < 4; k++) amdq[k] = amdq[k] + sfract * w4[k];
+done:
+    for (k = 0; k < 4; k++) {
+        double df = 0.0;
+        for (p = 0; p < 4; p++) df = df + s[p] * wave[4 * p + k];
+        apdq[k] = df - amdq[k];
+    }
+    return bad;
+}
+
+static int rpn2(const rp_t *rp, int ixy, const double *ql, const double *qr,
+                double *wave, double *s, double *amdq, double *apdq)
+{
+    switch (rp->id) {
+    case RP_ACOUSTICS: return rpn2_acoustics(rp, ixy, ql, qr, wave, s, amdq, apdq);
+    case RP_SHALLOW_ROE_EFIX: return rpn2_shallow(rp, ixy, ql, qr, wave, s, amdq, apdq);
+    default: return rpn2_euler(rp, ixy, ql, qr, wave, s, amdq, apdq);
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * Transverse Riemann solvers: split the normal fluctuation asdq at the edge
+ * between ql and qr into the parts going down (bmasdq) and up (bpasdq) in
+ * the transverse direction, with the transverse eigenstructure at the
+ * edge's Roe state.  bm[k] = sum_p min(sb_p,0) Wb_p[k], bp likewise with max.
+ * ---------------------------------------------------------------------- */
+static void rpt2_acoustics(const rp_t *rp, int ixy, const double *ql, const double *qr,
+                           const double *asdq, double *bm, double *bp)
+{
+    (void)ql; (void)qr;
+    const double cc = rp->pd[2], zz = rp->pd[3];
+    const int mu = ixy, mv = 3 - ixy;
+    double a1 = (-asdq[0] + zz * asdq[mv]) / (2.0 * zz);
+    double a2 = (asdq[0] + zz * asdq[mv]) / (2.0 * zz);
+    bm[0] = cc * a1 * zz; bm[mu] = 0.0; bm[mv] = -cc * a1;
+    bp[0] = cc * a2 * zz; bp[mu] = 0.0; bp[mv] = cc * a2;
+}
+
+static void split_sum(int m, int mw, const double *sb, const double *wb, double *bm, double *bp)
+{
+    for (int k = 0; k < m; k++) {
+        double lo = 0.0, hi = 0.0;
+        for (int p = 0; p < mw; p++) {
+            lo = lo + fmin(sb[p], 0.0) * wb[m * p + k];
+            hi = hi + fmax(sb[p], 0.0) * wb[m * p + k];
+        }
+        bm[k] = lo;
+        bp[k] = hi;
+    }
+}
+
+static void rpt2_shallow(const rp_t *rp, int ixy, const double *ql, const double *qr,
+                         const double *asdq, double *bm, double *bp)
+{
+    const double g = rp->pd[0];
+    const int mu = ixy, mv = 3 - ixy;
+    double hl = ql[0], hr = qr[0];
+    double hsqrtl = sqrt(hl), hsqrtr = sqrt(hr);
+    double hsq2 = hsqrtl + hsqrtr;
+    double ubar = (ql[mu] / hsqrtl + qr[mu] / hsqrtr) / hsq2;
+    double vbar = (ql[mv] / hsqrtl + qr[mv] / hsqrtr) / hsq2;
+    double hbar = (hl + hr) * 0.5;
+    double cbar = sqrt(g * hbar);
+    double a1 = ((vbar + cbar) * asdq[0] - asdq[mv]) * (0.5 / cbar);
+    double a2 = asdq[mu] - ubar * asdq[0];
+    double a3 = (-(vbar - cbar) * asdq[0] + asdq[mv]) * (0.5 / cbar);
+    double wb[9], sb[3];
+    wb[0] = a1; wb[mu] = a1 * ubar; wb[mv] = a1 * (vbar - cbar);
+    sb[0] = vbar - cbar;
+    wb[3] = 0.0; wb[3 + mu] = a2; wb[3 + mv] = 0.0;
+    sb[1] = vbar;
+    wb[6] = a3; wb[6 + mu] = a3 * ubar; wb[6 + mv] = a3 * (vbar + cbar);
+    sb[2] = vbar + cbar;
+    split_sum(3, 3, sb, wb, bm, bp);
+}
+
+static void rpt2_euler(const rp_t *rp, int ixy, const double *ql, const double *qr,
+                       const double *asdq, double *bm, double *bp)
+{
+    const double gamma1 = rp->pd[0] - 1.0;
+    const int mu = ixy, mv = 3 - ixy;
+    double rhsqrtl = sqrt(ql[0]), rhsqrtr = sqrt(qr[0]);
+    double pl = euler_pressure(gamma1, ql);
+    double pr = euler_pressure(gamma1, qr);
+    double rhsq2 = rhsqrtl + rhsqrtr;
+    double u = (ql[mu] / rhsqrtl + qr[mu] / rhsqrtr) / rhsq2;
+    double v = (ql[mv] / rhsqrtl + qr[mv] / rhsqrtr) / rhsq2;
+    double enth = ((ql[3] + pl) / rhsqrtl + (qr[3] + pr) / rhsqrtr) / rhsq2;
+    double u2v2 = u * u + v * v;
+    double c2 = gamma1 * (enth - 0.5 * u2v2);
+    double a = sqrt(c2);
+    double g1a2 = gamma1 / c2;
+    double euv = enth - u2v2;
+    double a3 = g1a2 * (euv * asdq[0] + u * asdq[mu] + v * asdq[mv] - asdq[3]);
+    double a2 = asdq[mu] - u * asdq[0];
+    double a4 = (asdq[mv] + (a - v) * asdq[0] - a * a3) / (2.0 * a);
+    double a1 = asdq[0] - a3 - a4;
+    double wb[16], sb[4];
+    wb[0] = a1; wb[mu] = a1 * u; wb[mv] = a1 * (v - a); wb[3] = a1 * (enth - v * a);
+    sb[0] = v - a;
+    wb[4] = a3; wb[4 + mu] = a3 * u; wb[4 + mv] = a3 * v; wb[7] = a3 * 0.5 * u2v2;
+    sb[1] = v;
+    wb[8] = 0.0; wb[8 + mu] = a2; wb[8 + mv] = 0.0; wb[11] = a2 * u;
+    sb[2] = v;
+    wb[12] = a4; wb[12 + mu] = a4 * u; wb[12 + mv] = a4 * (v + a); wb[15] = a4 * (enth + v * a);
+    sb[3] = v + a;
+    split_sum(4, 4, sb, wb, bm, bp);
+}
+
+static void rpt2(const rp_t *rp, int ixy, const double *ql, const double *qr,
+                 const double *asdq, double *bm, double *bp)
+{
+    switch (rp->id) {
+    case RP_ACOUSTICS: rpt2_acoustics(rp, ixy, ql, qr, asdq, bm, bp); return;
+    case RP_SHALLOW_ROE_EFIX: rpt2_shallow(rp, ixy, ql, qr, asdq, bm, bp); return;
+    default: rpt2_euler(rp, ixy, ql, qr, asdq, bm, bp); return;
+    }
+}
+
+/* Wave limiter function phi(theta) (FVMHP sec. 6.12; upstream philim):
+ * 1 minmod, 2 superbee, 3 van Leer, 4 monotonized centred (MC). */
+static double philim(int id, double r)
+{
+    double c;
+    switch (id) {
+    case 1: return fmax(0.0, fmin(1.0, r));
+    case 2: return fmax(0.0, fmax(fmin(1.0, 2.0 * r), fmin(2.0, r)));
+    case 3: return (r + fabs(r)) / (1.0 + fabs(r));
+    case 4:
+        c = (1.0 + r) / 2.0;
+        return fmax(0.0, fmin(c, fmin(2.0, 2.0 * r)));
+    default: return 1.0;
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * One 1D slice of n interior cells (cells -2..n+1 present), following
+ * flux2: Riemann problems at edges -1..n+1, Godunov fluctuations, CFL,
+ * limited second-order correction fluxes, transverse splitting.
+ * Edge e lies between cells e-1 and e.  Arrays are indexed with offset 2.
+ * Outputs (zeroed here):
+ *   qadd[c]  first-order update of cell c (already multiplied by dtdx)
+ *   fadd[e]  correction flux at edge e
+ *   g1[c], g2[c]  transverse correction fluxes at the low / high
+ *                 transverse edge of cell c of this slice
+ * ---------------------------------------------------------------------- */
+typedef struct {
+    double *wave, *s, *amdq, *apdq, *cqxx, *bm, *bp;
+} work_t;
+
+static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double dtdx,
+                       int order, int tw, const int *mthlim,
+                       double *qadd, double *fadd, double *g1, double *g2, double *cfl1d,
+                       const work_t *wk)
+{
+    const int m = rp->m, mw = rp->mw;
+    const int off = 2;
+    int e, k, p, bad = 0;
+#define Q(c) (q1d + (size_t)((c) + off) * m)
+#define W(e) (wk->wave + (size_t)((e) + off) * mw * m)
+#define S(e) (wk->s + (size_t)((e) + off) * mw)
+#define AM(e) (wk->amdq + (size_t)((e) + off) * m)
+#define AP(e) (wk->apdq + (size_t)((e) + off) * m)
+#define CQ(e) (wk->cqxx + (size_t)((e) + off) * m)
+#define BM(e) (wk->bm + (size_t)((e) + off) * m)
+#define BP(e) (wk->bp + (size_t)((e) + off) * m)
+#define A1(arr, c) ((arr) + (size_t)((c) + off) * m)
+
+    for (e = -1; e <= n + 1; e++)
+        bad |= rpn2(rp, ixy, Q(e - 1), Q(e), W(e), S(e), AM(e), AP(e));
+
+    for (e = -2; e <= n + 1; e++)
+        for (k = 0; k < m; k++) {
+            A1(qadd, e)[k] = 0.0;
+            A1(fadd, e)[k] = 0.0;
+            A1(g1, e)[k] = 0.0;
+            A1(g2, e)[k] = 0.0;
+        }
+
+    /* first-order (Godunov) updates */
+    for (e = 0; e <= n; e++)
+        for (k = 0; k < m; k++) {
+            A1(qadd, e)[k] = A1(qadd, e)[k] - dtdx * AP(e)[k];
+            A1(qadd, e - 1)[k] = A1(qadd, e - 1)[k] - dtdx * AM(e)[k];
+        }
+
+    /* Courant number over the edges of this slice */
+    double cfl = 0.0;
+    for (e = 0; e <= n; e++)
+        for (p = 0; p < mw; p++) {
+            double sp = S(e)[p];
+            cfl = fmax(cfl, fmax(dtdx * sp, -dtdx * sp));
+        }
+    *cfl1d = cfl;
+
+    if (order == 2) {
+        /* limit each wave family against its upwind neighbour; the neighbour
+         * waves used for theta are the unlimited ones */
+        for (p = 0; p < mw; p++) {
+            if (mthlim[p] == 0) continue;
+            double dotr = 0.0;
+            for (e = -1; e <= n; e++) {
+                double wnorm2 = 0.0, dotl = dotr;
+                dotr = 0.0;
+                const double *we = W(e) + p * m, *wn = W(e + 1) + p * m;
+                for (k = 0; k < m; k++) {
+                    wnorm2 = wnorm2 + we[k] * we[k];
+                    dotr = dotr + we[k] * wn[k];
+                }
+                if (e == -1) continue;
+                if (wnorm2 == 0.0) continue;
+                double r = (S(e)[p] > 0.0) ? dotl / wnorm2 : dotr / wnorm2;
+                double phi = philim(mthlim[p], r);
+                for (k = 0; k < m; k++) W(e)[p * m + k] = phi * W(e)[p * m + k];
+            }
+        }
+        double dtdxave = 0.5 * (dtdx + dtdx);
+        for (e = 0; e <= n; e++)
+            for (k = 0; k < m; k++) {
+                double c = 0.0;
+                for (p = 0; p < mw; p++) {
+                    double sa = fabs(S(e)[p]);
+                    c = c + sa * (1.0 - sa * dtdxave) * W(e)[p * m + k];
+                }
+                CQ(e)[k] = c;
+                A1(fadd, e)[k] = A1(fadd, e)[k] + 0.5 * c;
+            }
+    }
+
+    if (tw > 0) {
+        if (order == 2 && tw == 2)
+            for (e = 0; e <= n; e++)
+                for (k = 0; k < m; k++) {
+                    AM(e)[k] = AM(e)[k] + CQ(e)[k];
+                    AP(e)[k] = AP(e)[k] - CQ(e)[k];
+                }
+        const double h = 0.5 * dtdx;
+        for (e = 0; e <= n; e++) rpt2(rp, ixy, Q(e - 1), Q(e), AM(e), BM(e), BP(e));
+        for (e = 0; e <= n; e++)
+            for (k = 0; k < m; k++) {
+                A1(g1, e - 1)[k] = A1(g1, e - 1)[k] - h * BM(e)[k];
+                A1(g2, e - 1)[k] = A1(g2, e - 1)[k] - h * BP(e)[k];
+            }
+        for (e = 0; e <= n; e++) rpt2(rp, ixy, Q(e - 1), Q(e), AP(e), BM(e), BP(e));
+        for (e = 0; e <= n; e++)
+            for (k = 0; k < m; k++) {
+                A1(g1, e)[k] = A1(g1, e)[k] - h * BM(e)[k];
+                A1(g2, e)[k] = A1(g2, e)[k] - h * BP(e)[k];
+            }
+    }
+#undef Q
+#undef W
+#undef S
+#undef AM
+#undef AP
+#undef CQ
+#undef BM
+#undef BP
+#undef A1
+    return bad;
+}
+
+/* ------------------------------------------------------------------------
+ * Exported entry points (ctypes).
+ * ---------------------------------------------------------------------- */
+
+int gclaw_ref_shape(int rp_id, int *m, int *mw) { return rp_shape(rp_id, m, mw); }
+
+/* Ghost fill as PyClaw's _apply_bcs does it for a single-process run:
+ * x boundaries first over every row (y-ghost rows included), then y
+ * boundaries over every column (x-ghost columns included).  extrap copies the
+ * edge cell, periodic wraps, wall mirrors and negates the normal
+ * momentum/velocity component (component 1 for x, 2 for y).  q is (m,mx,my)
+ * Fortran order, qbc is (m,mx+2g,my+2g). */
+int gclaw_ref_fill_ghosts(int m, int mx, int my, int g, const int *bc_lower,
+                          const int *bc_upper, const double *q, double *qbc)
+{
+    if (m < 1 || m > MAXM || mx < g || my < g || g < 1) return ERR_ARG;
+    for (int d = 0; d < 2; d++)
+        if (bc_lower[d] < BC_EXTRAP || bc_lower[d] > BC_WALL || bc_upper[d] < BC_EXTRAP ||
+            bc_upper[d] > BC_WALL)
+            return ERR_ARG;
+    const int nx = mx + 2 * g, ny = my + 2 * g;
+#define QB(k, i, j) qbc[(size_t)(k) + (size_t)m * ((size_t)(i) + (size_t)nx * (size_t)(j))]
+    for (int j = 0; j < my; j++)
+        for (int i = 0; i < mx; i++)
+            for (int k = 0; k < m; k++)
+                QB(k, i + g, j + g) = q[(size_t)k + (size_t)m * ((size_t)i + (size_t)mx * j)];
+    /* x direction, all rows */
+    for (int j = 0; j < ny; j++)
+        for (int l = 0; l < g; l++) {
+            int src_lo, src_hi, neg_lo = 0, neg_hi = 0;
+            switch (bc_lower[0]) {
+            case BC_EXTRAP: src_lo = g; break;
+            case BC_PERIODIC: src_lo = l + mx; break;
+            default: src_lo = 2 * g - 1 - l; neg_lo = 1; break;
+            }
+            switch (bc_upper[0]) {
+            case BC_EXTRAP: src_hi = g + mx - 1; break;
+            case BC_PERIODIC: src_hi = g + l; break;
+            default: src_hi = g + mx - 1 - l; neg_hi = 1; break;
+            }
+            for (int k = 0; k < m; k++) {
+                double vlo = QB(k, src_lo, j), vhi = QB(k, src_hi, j);
+                QB(k, l, j) = (neg_lo && k == 1) ? -vlo : vlo;
+                QB(k, g + mx + l, j) = (neg_hi && k == 1) ? -vhi : vhi;
+            }
+        }
+    /* y direction, all columns */
+    for (int l = 0; l < g; l++)
+        for (int i = 0; i < nx; i++) {
+            int src_lo, src_hi, neg_lo = 0, neg_hi = 0;
+            switch (bc_lower[1]) {
+            case BC_EXTRAP: src_lo = g; break;
+            case BC_PERIODIC: src_lo = l + my; break;
+            default: src_lo = 2 * g - 1 - l; neg_lo = 1; break;
+            }
+            switch (bc_upper[1]) {
+            case BC_EXTRAP: src_hi = g + my - 1; break;
+            case BC_PERIODIC: src_hi = g + l; break;
+            default: src_hi = g + my - 1 - l; neg_hi = 1; break;
+            }
+            for (int k = 0; k < m; k++) {
+                double vlo = QB(k, i, src_lo), vhi = QB(k, i, src_hi);
+                QB(k, i, l) = (neg_lo && k == 2) ? -vlo : vlo;
+                QB(k, i, g + my + l) = (neg_hi && k == 2) ? -vhi : vhi;
+            }
+        }
+#undef QB
+    return 0;
+}
+
+/* One Riemann problem at an edge, for known-answer tests. */
+int gclaw_ref_rpn2(int rp_id, const double *pd, int ixy, const double *ql, const double *qr,
+                   double *wave, double *s, double *amdq, double *apdq)
+{
+    rp_t rp;
+    rp.id = rp_id;
+    if (rp_shape(rp_id, &rp.m, &rp.mw) || (ixy != 1 && ixy != 2)) return ERR_ARG;
+    memcpy(rp.pd, pd, sizeof rp.pd);
+    return rpn2(&rp, ixy, ql, qr, wave, s, amdq, apdq) ? ERR_NONPHYSICAL : 0;
+}
+
+int gclaw_ref_rpt2(int rp_id, const double *pd, int ixy, const double *ql, const double *qr,
+                   const double *asdq, double *bm, double *bp)
+{
+    rp_t rp;
+    rp.id = rp_id;
+    if (rp_shape(rp_id, &rp.m, &rp.mw) || (ixy != 1 && ixy != 2)) return ERR_ARG;
+    memcpy(rp.pd, pd, sizeof rp.pd);
+    rpt2(&rp, ixy, ql, qr, asdq, bm, bp);
+    return 0;
+}
+
+double gclaw_ref_philim(int id, double r) { return philim(id, r); }
+
+/* The classic unsplit step (step2).  qold and qnew are qbc-shaped
+ * (m, mx+2g, my+2g), Fortran order, ghosts of qold filled; g must be 2.
+ * qnew receives qold plus all updates (its ghost entries are qold's).
+ * pd: problem data (acoustics: rho, bulk, cc, zz; shallow: grav;
+ * euler: gamma, efix).  Returns 0, or ERR_NONPHYSICAL if a Riemann problem
+ * met a non-physical state. */
+int gclaw_ref_step2(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
+                    double *qnew, double dx, double dy, double dt, int order, int tw,
+                    const int *mthlim, double *cfl_out, int nthreads)
+{
+    rp_t rp;
+    rp.id = rp_id;
+    if (rp_shape(rp_id, &rp.m, &rp.mw) || g != 2 || mx < 2 || my < 2) return ERR_ARG;
+    if (order < 1 || order > 2 || tw < 0 || tw > 2) return ERR_ARG;
+    memcpy(rp.pd, pd, sizeof rp.pd);
+    const int m = rp.m, mw = rp.mw;
+    const int nx = mx + 2 * g, ny = my + 2 * g;
+    const double dtdx = dt / dx, dtdy = dt / dy;
+    const size_t qsize = (size_t)m * nx * ny;
+    memcpy(qnew, qold, qsize * sizeof(double));
+
+    /* per-slice outputs: [slice][cell(+2 offset)][k] */
+    const int nmax = (mx > my ? mx : my) + 4;
+    const int nslx = my + 2, nsly = mx + 2;
+    const int nsl = nslx > nsly ? nslx : nsly;
+    const size_t per = (size_t)nmax * m;
+    double *QA = malloc(sizeof(double) * per * nsl);
+    double *FA = malloc(sizeof(double) * per * nsl);
+    double *G1 = malloc(sizeof(double) * per * nsl);
+    double *G2 = malloc(sizeof(double) * per * nsl);
+    double *cfls = malloc(sizeof(double) * nsl);
+    if (!QA || !FA || !G1 || !G2 || !cfls) {
+        free(QA); free(FA); free(G1); free(G2); free(cfls);
+        return ERR_ALLOC;
+    }
+    if (nthreads < 1) nthreads = 1;
+    int bad = 0;
+    double cfl = 0.0;
+
+    for (int ixy = 1; ixy <= 2; ixy++) {
+        const int n = (ixy == 1) ? mx : my;
+        const int ns = (ixy == 1) ? nslx : nsly;
+        const double dtdn = (ixy == 1) ? dtdx : dtdy;
+#pragma omp parallel num_threads(nthreads) reduction(| : bad)
+        {
+            work_t wk;
+            double *q1d = malloc(sizeof(double) * per);
+            wk.wave = malloc(sizeof(double) * (size_t)nmax * mw * m);
+            wk.s = malloc(sizeof(double) * (size_t)nmax * mw);
+            wk.amdq = malloc(sizeof(double) * per);
+            wk.apdq = malloc(sizeof(double) * per);
+            wk.cqxx = malloc(sizeof(double) * per);
+            wk.bm = malloc(sizeof(double) * per);
+            wk.bp = malloc(sizeof(double) * per);
+#pragma omp for schedule(static)
+            for (int sl = 0; sl < ns; sl++) {
+                /* slice index sl -> row j = sl-1 (x-sweep) or column i = sl-1 */
+                for (int c = -2; c < n + 2; c++)
+                    for (int k = 0; k < m; k++) {
+                        size_t src = (ixy == 1)
+                                         ? (size_t)k + (size_t)m * ((size_t)(c + g) + (size_t)nx * (sl - 1 + g))
+                                         : (size_t)k + (size_t)m * ((size_t)(sl - 1 + g) + (size_t)nx * (c + g));
+                        q1d[(size_t)(c + 2) * m + k] = qold[src];
+                    }
+                bad |= flux2_slice(&rp, ixy, n, q1d, dtdn, order, tw, mthlim, QA + per * sl,
+                                   FA + per * sl, G1 + per * sl, G2 + per * sl, &cfls[sl], &wk);
+            }
+            free(q1d); free(wk.wave); free(wk.s); free(wk.amdq); free(wk.apdq);
+            free(wk.cqxx); free(wk.bm); free(wk.bp);
+        }
+        for (int sl = 0; sl < ns; sl++) cfl = fmax(cfl, cfls[sl]);
+
+        /* ordered accumulation: for cell (i,j) the slice before, the own slice,
+         * the slice after */
+        const double dtdt = (ixy == 1) ? dtdy : dtdx; /* transverse dt/d */
+        const int nt = (ixy == 1) ? my : mx;         /* number of slices' interior */
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+        for (int t = 0; t < nt; t++) {
+            const int sl = t + 1; /* slice of interior index t */
+            for (int c = 0; c < n; c++) {
+                size_t dst = (ixy == 1) ? (size_t)m * ((size_t)(c + g) + (size_t)nx * (t + g))
+                                        : (size_t)m * ((size_t)(t + g) + (size_t)nx * (c + g));
+                const double *g2prev = G2 + per * (sl - 1) + (size_t)(c + 2) * m;
+                const double *g1next = G1 + per * (sl + 1) + (size_t)(c + 2) * m;
+                const double *qa = QA + per * sl + (size_t)(c + 2) * m;
+                const double *fa0 = FA + per * sl + (size_t)(c + 2) * m;
+                const double *fa1 = fa0 + m;
+                const double *g1o = G1 + per * sl + (size_t)(c + 2) * m;
+                const double *g2o = G2 + per * sl + (size_t)(c + 2) * m;
+                for (int k = 0; k < m; k++) {
+                    double v = qnew[dst + k];
+                    v = v + dtdt * g2prev[k];
+                    v = v + qa[k] - dtdn * (fa1[k] - fa0[k]) - dtdt * (g2o[k] - g1o[k]);
+                    v = v - dtdt * g1next[k];
+                    qnew[dst + k] = v;
+                }
+            }
+        }
+    }
+    free(QA); free(FA); free(G1); free(G2); free(cfls);
+    *cfl_out = cfl;
+    return bad ? ERR_NONPHYSICAL : 0;
+}
+
+/* Convenience: ghost fill + step on interior-shaped arrays (m, mx, my). */
+int gclaw_ref_step(int rp_id, const double *pd, int mx, int my, const double *q, double *qout,
+                   double dx, double dy, double dt, int order, int tw, const int *mthlim,
+                   const int *bc_lower, const int *bc_upper, double *cfl_out, int nthreads)
+{
+    int m, mw;
+    if (rp_shape(rp_id, &m, &mw)) return ERR_ARG;
+    const int g = 2, nx = mx + 4, ny = my + 4;
+    size_t nb = (size_t)m * nx * ny;
+    double *qa = malloc(sizeof(double) * nb), *qb = malloc(sizeof(double) * nb);
+    if (!qa || !qb) {
+        free(qa); free(qb);
+        return ERR_ALLOC;
+    }
+    int rc = gclaw_ref_fill_ghosts(m, mx, my, g, bc_lower, bc_upper, q, qa);
+    if (rc == 0)
+        rc = gclaw_ref_step2(rp_id, pd, g, mx, my, qa, qb, dx, dy, dt, order, tw, mthlim, cfl_out,
+                             nthreads);
+    if (rc == 0 || rc == ERR_NONPHYSICAL)
+        for (int j = 0; j < my; j++)
+            for (int i = 0; i < mx; i++)
+                for (int k = 0; k < m; k++)
+                    qout[(size_t)k + (size_t)m * ((size_t)i + (size_t)mx * j)] =
+                        qb[(size_t)k + (size_t)m * ((size_t)(i + g) + (size_t)nx * (j + g))];
+    free(qa);
+    free(qb);
+    return rc;
+}

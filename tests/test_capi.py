@@ -1,0 +1,101 @@
+"""libgclaw.so loads without a GPU, exports every function include/gclaw.h
+declares, and its host-side argument checks behave (no kernel is launched)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from clawpack_gb300 import _lib
+from clawpack_gb300.device import make_solver_struct
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "gclaw.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_]+\s*\*?\s*(gclaw_[a-z0-9_]+)\s*\(", src,
+                                 flags=re.M)))
+
+
+@pytest.mark.parametrize("strict", [False, True])
+def test_exports_every_declared_symbol(strict):
+    L = _lib.lib(strict)
+    names = declared_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
+
+
+def _offsets_from_header(struct_name):
+    src = open(HEADER).read()
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (struct_name, struct_name), src,
+                     re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        typ, rest = re.match(r"((?:unsigned\s+)?(?:long\s+long|int|double))\s+(.*)", decl).groups()
+        for item in rest.split(","):
+            item = item.strip()
+            m = re.match(r"([a-z_0-9]+)(?:\[([A-Z_0-9]+)\])?", item)
+            fields.append(m.group(1))
+    return fields
+
+
+def test_struct_layouts_match_header():
+    for cls, name in ((_lib.GclawSolver, "gclaw_solver"), (_lib.GclawCtrl, "gclaw_ctrl")):
+        assert [f[0] for f in cls._fields_] == _offsets_from_header(name)
+    assert ctypes.sizeof(_lib.GclawCtrl) == 144
+    assert ctypes.sizeof(_lib.GclawCtrl) <= 256
+
+
+def good_solver(**kw):
+    args = dict(rp_id=2, mx=8, my=8, dx=0.1, dy=0.1, bc_lower=[3, 3], bc_upper=[3, 3],
+                mthlim=[4, 4, 4], order=2, tw=2, precision=0, problem_data=[1.0])
+    args.update(kw)
+    return make_solver_struct(**args)
+
+
+def test_check_accepts_valid_and_rejects_invalid():
+    L = _lib.lib()
+    assert L.gclaw_check(ctypes.byref(good_solver())) == _lib.OK
+    bad = [dict(rp_id=9), dict(mx=1), dict(dx=0.0), dict(order=3), dict(tw=5),
+           dict(precision=7), dict(problem_data=[0.0]), dict(bc_lower=[2, 3]),
+           dict(bc_lower=[4, 3])]
+    for kw in bad:
+        assert L.gclaw_check(ctypes.byref(good_solver(**kw))) == _lib.ERR_ARG, kw
+    assert L.gclaw_check(ctypes.byref(good_solver(bc_lower=[0, 3]))) == _lib.ERR_UNSUPPORTED
+    assert L.gclaw_check(ctypes.byref(good_solver(mthlim=[9, 4, 4]))) == _lib.ERR_UNSUPPORTED
+    assert L.gclaw_check(None) == _lib.ERR_ARG
+
+
+def test_step_entry_points_reject_bad_arguments_before_any_launch():
+    L = _lib.lib()
+    s = good_solver()
+    cfl = ctypes.c_double()
+    assert L.gclaw_step2(ctypes.byref(s), None, None, 0.1, None, ctypes.byref(cfl), None) == \
+        _lib.ERR_ARG
+    assert L.gclaw_step(ctypes.byref(s), None, None, 0.1, None, None) == _lib.ERR_ARG
+    assert L.gclaw_advance(ctypes.byref(s), None, None, None, 1, None) == _lib.ERR_ARG
+    assert L.gclaw_ctrl_init(None, 0.0, 0.1, 1.0, 1.0, 0.9, 1e99, 10, -1, 1, None) == \
+        _lib.ERR_ARG
+
+
+def test_shapes_versions_workspace():
+    L = _lib.lib()
+    m, mw = ctypes.c_int(), ctypes.c_int()
+    for rp, shape in ((1, (3, 2)), (2, (3, 3)), (3, (4, 4))):
+        assert L.gclaw_rp_shape(rp, ctypes.byref(m), ctypes.byref(mw)) == 0
+        assert (m.value, mw.value) == shape
+    assert L.gclaw_rp_shape(0, ctypes.byref(m), ctypes.byref(mw)) == _lib.ERR_ARG
+    assert b"sm_103a" in L.gclaw_version()
+    for st in (0, -1, -2, -4, -5, 2, 3, 4):
+        assert L.gclaw_strerror(st) and L.gclaw_strerror(st) != b"unknown status"
+    s = good_solver(mx=100, my=50)
+    assert L.gclaw_evolve_workspace_bytes(ctypes.byref(s)) >= 256 + 2 * 3 * 100 * 50 * 8

@@ -1,0 +1,78 @@
+"""The PyClaw-compatible API surface (no GPU needed for these checks)."""
+import numpy as np
+import pytest
+
+from clawpack_gb300 import pyclaw, riemann, workloads
+
+
+def test_solver_defaults_follow_pyclaw():
+    s = pyclaw.ClawSolver2D(riemann.euler_4wave_2D)
+    assert (s.num_eqn, s.num_waves) == (4, 4)
+    assert s.dimensional_split is True
+    assert s.transverse_waves == s.trans_inc == 1
+    assert s.order == 2 and s.num_ghost == 2
+    assert s.limiters == pyclaw.limiters.tvd.minmod
+    assert s.cfl_max == 1.0 and s.cfl_desired == 0.9 and s.dt_initial == 0.1
+    assert s.max_steps == 10000 and s.dt_variable
+    assert s.kernel_language == "CUDA"
+    assert s._mthlim == [1, 1, 1, 1]
+    s.limiters = [4, 2, 2, 4]
+    assert s._mthlim == [4, 2, 2, 4]
+    s.limiters = [1, 2]
+    with pytest.raises(ValueError):
+        s._mthlim
+
+
+def test_bc_and_limiter_ids():
+    assert (pyclaw.BC.custom, pyclaw.BC.extrap, pyclaw.BC.periodic, pyclaw.BC.wall) == (0, 1, 2, 3)
+    t = pyclaw.limiters.tvd
+    assert (t.minmod, t.superbee, t.vanleer, t.MC) == (1, 2, 3, 4)
+    assert riemann.static.num_eqn["shallow_roe_with_efix_2D"] == 3
+
+
+def test_grid_and_state():
+    x = pyclaw.Dimension(-1.0, 1.0, 4, name="x")
+    y = pyclaw.Dimension(0.0, 1.0, 2, name="y")
+    d = pyclaw.Domain([x, y])
+    st = pyclaw.State(d, 3)
+    assert st.q.shape == (3, 4, 2) and st.q.flags.f_contiguous
+    X, Y = st.grid.p_centers
+    assert X.shape == (4, 2)
+    np.testing.assert_allclose(X[:, 0], [-0.75, -0.25, 0.25, 0.75])
+    assert st.grid.x is x and d.grid.delta == [0.5, 0.5]
+
+
+def test_unsupported_options_fail_loudly():
+    claw = workloads.make_claw(workloads.acoustics_radial(8, 8))
+    s = claw.solver
+    st = claw.solution.state
+    s.dimensional_split = True
+    with pytest.raises(NotImplementedError):
+        s.solver_struct(st)
+    s.dimensional_split = False
+    s.kernel_language = "Fortran"
+    with pytest.raises(NotImplementedError):
+        s.solver_struct(st)
+    s.kernel_language = "CUDA"
+    s.bc_lower[0] = pyclaw.BC.custom
+    with pytest.raises(NotImplementedError):
+        s.solver_struct(st)
+
+
+def test_problem_data_mapping():
+    claw = workloads.make_claw(workloads.acoustics_radial(8, 8))
+    s, st = claw.solver, claw.solution.state
+    del st.problem_data["cc"], st.problem_data["zz"]
+    ss = s.solver_struct(st)
+    assert list(ss.problem_data)[:4] == [1.0, 4.0, 2.0, 2.0]
+    claw = workloads.make_claw(workloads.euler_quadrants(8, 8))
+    ss = claw.solver.solver_struct(claw.solution.state)
+    assert list(ss.problem_data)[:2] == [1.4, 1.0]
+
+
+def test_workloads_shapes():
+    w = workloads.shallow_dam_break(64, 32)
+    assert w.q0.shape == (3, 64, 32) and set(np.unique(w.q0[0])) == {1.0, 2.0}
+    e = workloads.euler_quadrants(16, 16)
+    assert len(e.meta["states"]) == 4 and e.q0.shape == (4, 16, 16)
+    assert np.all(e.q0[0] > 0)
