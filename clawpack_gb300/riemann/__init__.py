@@ -16,8 +16,11 @@ from . import static
 
 
 def _descriptor(name, rp_id):
+    # cparam plays the role of the f2py module's Fortran common block, which
+    # PyClaw fills from state.problem_data before stepping.
     return SimpleNamespace(__name__=f"clawpack_gb300.riemann.{name}", name=name, rp_id=rp_id,
-                           num_eqn=static.num_eqn[name], num_waves=static.num_waves[name])
+                           num_eqn=static.num_eqn[name], num_waves=static.num_waves[name],
+                           cparam=SimpleNamespace())
 
 
 acoustics_2D = _descriptor("acoustics_2D", _lib.RP_ACOUSTICS_2D)

@@ -1,0 +1,63 @@
+"""Run one benchmark problem on the GPU and report its step time.
+
+    python -m clawpack_gb300.run_case --workload shallow --mx 2048 --steps 100 \
+        --precision fp64
+
+Advances the chosen problem by --warmup then --steps device-controlled steps
+(one step kernel each) and prints one JSON line with the mean step time from
+CUDA events.  Used for profiling captures and quick size sweeps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+
+import torch
+
+from . import workloads
+from .device import DeviceProblem
+
+
+def make_workload(name, mx, my):
+    if name == "shallow":
+        return workloads.shallow_dam_break(mx, my)
+    if name == "euler":
+        return workloads.euler_quadrants(mx, my)
+    if name == "acoustics":
+        return workloads.acoustics_radial(mx, my)
+    raise ValueError(name)
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("--workload", default="shallow", choices=["shallow", "euler", "acoustics"])
+    p.add_argument("--mx", type=int, default=2048)
+    p.add_argument("--my", type=int, default=None)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    a = p.parse_args(argv)
+    w = make_workload(a.workload, a.mx, a.my or a.mx)
+    dev = DeviceProblem(w.solver_struct(0 if a.precision == "fp64" else 1))
+    dev.upload(w.q0)
+    dev.ctrl_init(0.0, w.dt_initial, math.inf, cfl_max=w.cfl_max, cfl_desired=w.cfl_desired,
+                  max_steps=10 ** 9)
+    dev.advance(a.warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    dev.advance(a.steps)
+    e1.record()
+    c = dev.read_ctrl()
+    ms = e0.elapsed_time(e1) / max(a.steps, 1)
+    cells = w.mx * w.my
+    print(json.dumps({"workload": w.name, "mx": w.mx, "my": w.my, "precision": a.precision,
+                      "steps": a.steps, "ms_per_step": ms,
+                      "gcell_updates_per_s": cells / (ms * 1e-3) * 1e-9 if ms > 0 else None,
+                      "accepted": c.numsteps, "status": c.status, "cfl": c.cfl}))
+    return 0 if c.status == 0 else 1
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -136,3 +136,30 @@ def test_negative_pressure_reports_nonphysical(cuda):
     q[3, 4, 4] = 0.01 * q[3, 4, 4] - 10.0  # E so low that the Roe c^2 < 0
     qg, c = gpu_step(3, q, 0.05, 0.05, 0.001, [1, 1], [1, 1])
     assert c.status == _lib.NONPHYSICAL
+
+
+@pytest.mark.parametrize("rp", [1, 2, 3])
+def test_f2py_shaped_step2_dropin(cuda, oracle, rp):
+    """clawpack_gb300.classic2.step2 called exactly as PyClaw calls the f2py
+    classic2.step2, with numpy qbc arrays and the riemann module's cparam."""
+    from clawpack_gb300 import classic2, riemann
+
+    mod = {1: riemann.acoustics_2D, 2: riemann.shallow_roe_with_efix_2D,
+           3: riemann.euler_4wave_2D}[rp]
+    names = {1: dict(rho=1.0, bulk=4.0, cc=2.0, zz=2.0), 2: dict(grav=1.0),
+             3: dict(gamma=1.4, efix=True)}[rp]
+    for k, v in names.items():
+        setattr(mod.cparam, k, v)
+    rng = np.random.default_rng(300 + rp)
+    mx, my = 33, 21
+    q = random_state(rp, mx, my, rng)
+    qbc = oracle.fill_ghosts(q, [1, 3], [1, 3])
+    qnew = qbc.copy(order="F")
+    method = np.array([1, 2, 2, 0, 1, 0, 0])
+    mw = SHAPES[rp][1]
+    out, cfl = classic2.step2(max(mx, my), 2, mx, my, qbc, qnew, None, 0.05, 0.04, 0.002, method,
+                              [4] * mw, False, mod, mod)
+    ref_q, ref_cfl = oracle.step2(rp, PD[rp], qbc, 0.05, 0.04, 0.002, 2, 2, [4] * 4)
+    assert out is qnew
+    assert rel_l1(out[:, 2:-2, 2:-2], ref_q[:, 2:-2, 2:-2]) <= 1e-13
+    assert abs(cfl - ref_cfl) <= 1e-14 * ref_cfl
