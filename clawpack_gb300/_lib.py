@@ -27,6 +27,8 @@ ERR_ARG = -1
 ERR_CUDA = -2
 ERR_UNSUPPORTED = -4
 ERR_WORKSPACE = -5
+ERR_TOO_LARGE = -6
+NOALLOC_MAX_BLOCKS = 131072
 NONPHYSICAL = 2
 CFL_FIXED_DT = 3
 MAX_STEPS = 4
@@ -98,6 +100,7 @@ SIGNATURES = {
     "gclaw_step_workspace_bytes": (_SZ, [_SP]),
     "gclaw_step_host": (_I, [_SP, _P, _P, _D, _P, _SZ, ctypes.POINTER(_D), _P]),
     "gclaw_evolve_workspace_bytes": (_SZ, [_SP]),
+    "gclaw_step2_noalloc": (_I, [_SP, _P, _P, _D, ctypes.POINTER(_D), _P]),
     "gclaw_evolve_host": (_I, [_SP, _P, _P, _D, _D, _D, _I, _D, _D, _D, _I, _P, _SZ, _I,
                                ctypes.POINTER(GclawCtrl), _P]),
 }

@@ -556,6 +556,9 @@ const char *gclaw_strerror(int st) {
     case GCLAW_ERR_CUDA: return "CUDA error";
     case GCLAW_ERR_UNSUPPORTED: return "unsupported option";
     case GCLAW_ERR_WORKSPACE: return "workspace too small";
+    case GCLAW_ERR_TOO_LARGE:
+        return "grid needs more thread blocks than the no-allocation scratch holds "
+               "(GCLAW_NOALLOC_MAX_BLOCKS)";
     case GCLAW_NONPHYSICAL: return "non-physical state (NaN wave speed or negative sound speed squared)";
     case GCLAW_CFL_FIXED_DT: return "CFL too large with fixed dt";
     case GCLAW_MAX_STEPS: return "maximum number of time steps taken";
@@ -767,3 +770,246 @@ int gclaw_evolve_host(const gclaw_solver *s, const double *q_host, double *q_out
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// gclaw_step2_noalloc: the classic2.step2 drop-in without a caller workspace.
+//
+// gclaw_step2 borrows a gclaw_ctrl from the caller as the scratch of its
+// Courant-number reduction.  Some callers have no way to provide one: a
+// Fortran or C host program that reaches the step through f2py or ctypes
+// holding only the device arrays of the state it was handed, a process
+// whose device memory is owned by another framework's caching allocator
+// and must not grow behind its back, or code that has to stay
+// allocation-free after start-up.  This variant keeps its scratch in
+// g_noalloc_scratch, a file-scope __device__ array that every GPU loading
+// the library holds until the process exits:
+//   256-byte header (block counter, non-physical flag, CFL, status) +
+//   one 16-byte slot per thread block (max |s| on its x- and y-edges),
+//   GCLAW_NOALLOC_MAX_BLOCKS slots: 2 MiB + 256 B in total.
+// Each thread block writes its slot; the last block to finish reduces all
+// slots.  The caller passes the input and output states only.
+// ===========================================================================
+namespace gclaw {
+
+constexpr size_t NOALLOC_HEADER_BYTES = 256;
+constexpr size_t NOALLOC_SCRATCH_BYTES =
+    NOALLOC_HEADER_BYTES + 16 * (size_t)GCLAW_NOALLOC_MAX_BLOCKS;
+
+struct NoallocHeader {
+    unsigned int blocks_done;  // last-block counter, zero between calls
+    unsigned int flags;        // non-physical flag of this call
+    int status;                // GCLAW_OK or GCLAW_NONPHYSICAL
+    int pad;
+    double cfl;                // Courant number of this call
+};
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+template <template <typename> class RPT, typename T, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT)
+    step_kernel_noalloc(const StepArgs a, const typename RPT<T>::Params P,
+                        unsigned char *__restrict__ scratch) {
+    using RP = RPT<T>;
+    using TL = Tile<RP, TX, TY>;
+    using A = T;
+    constexpr int M = RP::M;
+    constexpr int NC = (TX * TY + NT - 1) / NT;
+    constexpr bool FP64 = sizeof(T) == 8;
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *QS = reinterpret_cast<T *>(smem_raw);
+    T *EA = QS + M * TL::QN;
+    T *EB = EA + TL::EAW * TL::NE1;
+    __shared__ double s_red[2][NT / 32];
+    __shared__ int s_last;
+
+    const double dt = a.dt;
+    const double dtdx = dt / a.dx, dtdy = dt / a.dy;
+    const T tdtdx = (T)dtdx, tdtdy = (T)dtdy;
+    const double *__restrict__ qin = a.qin[0];
+    double *__restrict__ qout = a.qout[0];
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+
+    for (int idx = threadIdx.x; idx < TL::QN * M; idx += NT) {
+        const int k = idx % M, cell = idx / M;
+        const int cx = cell % TL::QW, cy = cell / TL::QW;
+        QS[(k * TL::QH + cy) * TL::QW + cx] = (T)load_q<M>(a, qin, k, i0 - 2 + cx, j0 - 2 + cy);
+    }
+    __syncthreads();
+
+    A acc[NC][M];
+#pragma unroll
+    for (int t = 0; t < NC; t++) {
+        const int n = threadIdx.x + t * NT;
+        const int ci = n % TX, cj = n / TX;
+#pragma unroll
+        for (int k = 0; k < M; k++)
+            acc[t][k] = (FP64 && n < TX * TY) ? QS[(k * TL::QH + cj + 2) * TL::QW + ci + 2] : (A)0;
+    }
+
+    T smax_x = (T)0, smax_y = (T)0;
+    bool bad = false;
+    phase_rpn2<RP, T, 1, TX, TY, NT>(P, QS, EA, i0, j0, a.mx, a.my, smax_x, bad);
+    __syncthreads();
+    phase_limit<RP, T, 1, TX, TY, NT>(P, EA, EB, a.mthlim, a.order, a.tw, tdtdx);
+    __syncthreads();
+    phase_accum<RP, T, A, 1, TX, TY, NT, NC>(EA, EB, acc, tdtdx, tdtdy);
+    __syncthreads();
+    phase_rpn2<RP, T, 2, TX, TY, NT>(P, QS, EA, i0, j0, a.mx, a.my, smax_y, bad);
+    __syncthreads();
+    phase_limit<RP, T, 2, TX, TY, NT>(P, EA, EB, a.mthlim, a.order, a.tw, tdtdy);
+    __syncthreads();
+    phase_accum<RP, T, A, 2, TX, TY, NT, NC>(EA, EB, acc, tdtdy, tdtdx);
+
+    const int onx = a.ghosted ? a.mx + 4 : a.mx, ooff = a.ghosted ? 2 : 0;
+#pragma unroll
+    for (int t = 0; t < NC; t++) {
+        const int n = threadIdx.x + t * NT;
+        if (n >= TX * TY) break;
+        const int gi = i0 + n % TX, gj = j0 + n / TX;
+        if (gi < a.mx && gj < a.my) {
+            const size_t o = (size_t)M * ((size_t)(gi + ooff) + (size_t)onx * (size_t)(gj + ooff));
+#pragma unroll
+            for (int k = 0; k < M; k++)
+                qout[o + k] = FP64 ? (double)acc[t][k] : __ldg(qin + o + k) + (double)acc[t][k];
+        }
+    }
+
+    double bx = (double)smax_x, by = (double)smax_y;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        bx = fmax(bx, __shfl_xor_sync(0xffffffffu, bx, off));
+        by = fmax(by, __shfl_xor_sync(0xffffffffu, by, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_red[0][threadIdx.x >> 5] = bx;
+        s_red[1][threadIdx.x >> 5] = by;
+    }
+    const int anybad = __syncthreads_or(bad ? 1 : 0);
+    NoallocHeader *hdr = reinterpret_cast<NoallocHeader *>(scratch);
+    double2 *slots = reinterpret_cast<double2 *>(scratch + NOALLOC_HEADER_BYTES);
+    const unsigned nblocks = gridDim.x * gridDim.y;
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < NT / 32; w++) {
+            bx = fmax(bx, s_red[0][w]);
+            by = fmax(by, s_red[1][w]);
+        }
+        slots[blockIdx.y * gridDim.x + blockIdx.x] = make_double2(bx, by);
+        if (anybad) atomicOr(&hdr->flags, 1u);
+        __threadfence();
+        s_last = (atomicAdd(&hdr->blocks_done, 1u) == nblocks - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double mx = 0.0, my = 0.0;
+    for (unsigned b = threadIdx.x; b < nblocks; b += NT) {
+        const double2 v = __ldcg(&slots[b]);
+        mx = fmax(mx, v.x);
+        my = fmax(my, v.y);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+        my = fmax(my, __shfl_xor_sync(0xffffffffu, my, off));
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+        s_red[0][threadIdx.x >> 5] = mx;
+        s_red[1][threadIdx.x >> 5] = my;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < NT / 32; w++) {
+            mx = fmax(mx, s_red[0][w]);
+            my = fmax(my, s_red[1][w]);
+        }
+        const double cx = dtdx * mx, cy = dtdy * my;
+        hdr->cfl = cx > cy ? cx : cy;
+        hdr->status = atomicExch(&hdr->flags, 0u) ? GCLAW_NONPHYSICAL : GCLAW_OK;
+        hdr->blocks_done = 0u;
+    }
+}
+
+// Device address of g_noalloc_scratch, looked up once per device.
+static void *g_noalloc_ptr[64];
+
+template <template <typename> class RPT, typename T, int TX, int TY, int NT>
+static int launch_noalloc(const gclaw_solver *s, const StepArgs &a, cudaStream_t st,
+                          unsigned char *scratch) {
+    using RP = RPT<T>;
+    using TL = Tile<RP, TX, TY>;
+    constexpr size_t smem = TL::template smem_bytes<T>();
+    auto kern = step_kernel_noalloc<RPT, T, TX, TY, NT>;
+    const long long nblocks =
+        (long long)((s->mx + TX - 1) / TX) * (long long)((s->my + TY - 1) / TY);
+    if (nblocks > GCLAW_NOALLOC_MAX_BLOCKS) return GCLAW_ERR_TOO_LARGE;
+    static unsigned long long configured = 0ull;  // one bit per device ordinal
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return GCLAW_ERR_CUDA;
+    if (!(configured & (1ull << dev))) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return GCLAW_ERR_CUDA;
+        configured |= 1ull << dev;
+    }
+    if (cudaMemsetAsync(scratch, 0, NOALLOC_HEADER_BYTES, st) != cudaSuccess)
+        return GCLAW_ERR_CUDA;
+    const typename RP::Params P = RP::make(s->problem_data);
+    dim3 grid((s->mx + TX - 1) / TX, (s->my + TY - 1) / TY);
+    kern<<<grid, NT, smem, st>>>(a, P, scratch);
+    return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
+}
+
+}  // namespace gclaw
+
+extern "C" int gclaw_step2_noalloc(const gclaw_solver *s, const double *qold_dev,
+                                   double *qnew_dev, double dt, double *cfl_out, void *stream) {
+    int rc = gclaw_check(s);
+    if (rc) return rc;
+    if (!qold_dev || !qnew_dev || !cfl_out || !(dt > 0.0)) return GCLAW_ERR_ARG;
+    const bool f64 = s->precision == GCLAW_PREC_FP64;
+    const long long tiles_x = (s->mx + 31) / 32, tiles_y = (s->my + (f64 ? 7 : 15)) / (f64 ? 8 : 16);
+    if (tiles_x * tiles_y > GCLAW_NOALLOC_MAX_BLOCKS) return GCLAW_ERR_TOO_LARGE;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return GCLAW_ERR_CUDA;
+    if (!g_noalloc_ptr[dev]) {
+        // first call on this device: the device address of the file-scope
+        // scratch (the host-side name is only a stand-in for it)
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
+            return GCLAW_ERR_CUDA;
+        g_noalloc_ptr[dev] = p;
+    }
+    unsigned char *scratch = (unsigned char *)g_noalloc_ptr[dev];
+    StepArgs a{};
+    fill_args(s, a);
+    a.qin[0] = a.qin[1] = qold_dev;
+    a.qout[0] = a.qout[1] = qnew_dev;
+    a.ctrl = nullptr;
+    a.dt = dt;
+    a.ghosted = 1;
+    a.ctrl_mode = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (s->rp) {
+    case GCLAW_RP_ACOUSTICS_2D:
+        rc = f64 ? launch_noalloc<RpAcoustics, double, 32, 8, 256>(s, a, st, scratch)
+                 : launch_noalloc<RpAcoustics, float, 32, 16, 256>(s, a, st, scratch);
+        break;
+    case GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D:
+        rc = f64 ? launch_noalloc<RpShallow, double, 32, 8, 256>(s, a, st, scratch)
+                 : launch_noalloc<RpShallow, float, 32, 16, 256>(s, a, st, scratch);
+        break;
+    default:
+        rc = f64 ? launch_noalloc<RpEuler, double, 32, 8, 256>(s, a, st, scratch)
+                 : launch_noalloc<RpEuler, float, 32, 16, 256>(s, a, st, scratch);
+        break;
+    }
+    if (rc) return rc;
+    NoallocHeader h;
+    if (cudaMemcpyAsync(&h, scratch, sizeof h, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return GCLAW_ERR_CUDA;
+    *cfl_out = h.cfl;
+    return h.status;
+}

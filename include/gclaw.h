@@ -58,6 +58,7 @@ extern "C" {
 #define GCLAW_ERR_CUDA (-2)
 #define GCLAW_ERR_UNSUPPORTED (-4)
 #define GCLAW_ERR_WORKSPACE (-5)
+#define GCLAW_ERR_TOO_LARGE (-6) /* grid exceeds GCLAW_NOALLOC_MAX_BLOCKS thread blocks */
 #define GCLAW_NONPHYSICAL 2  /* NaN Courant number or negative Euler c^2 */
 #define GCLAW_CFL_FIXED_DT 3 /* step rejected while dt_variable = 0 */
 #define GCLAW_MAX_STEPS 4    /* attempts reached max_steps before tend */
@@ -185,6 +186,27 @@ int gclaw_evolve_host(const gclaw_solver *s, const double *q_host, double *q_out
                       double dt, double t_end, int max_accepted, double cfl_max,
                       double cfl_desired, double dt_max, int max_steps, void *ws_dev,
                       size_t ws_bytes, int batch, gclaw_ctrl *ctrl_out, void *stream);
+
+/* Allocation-free variant of gclaw_step2 (no counterpart in the reference,
+ * whose Fortran step needs no device memory).  For callers that cannot
+ * allocate device memory or hand over a workspace -- a Fortran/C host code
+ * holding only the state arrays it was given, or a process whose device
+ * memory belongs to another framework's caching allocator.  Same arguments
+ * and results as gclaw_step2 minus ws_dev: the reduction scratch is a
+ * file-scope __device__ array of 2 MiB + 256 B that every GPU loading the
+ * library keeps until the process exits, with one slot per thread block, so
+ * grids needing more than GCLAW_NOALLOC_MAX_BLOCKS thread blocks (32x8 cells
+ * each in FP64, 32x16 in FP32-bulk; e.g. 33.5 M cells in FP64) are rejected
+ * with GCLAW_ERR_TOO_LARGE before any launch.  The call allocates nothing
+ * (no cudaMalloc/cudaFree); it clears the scratch header on the stream,
+ * launches, reads the Courant number back and synchronises the stream.  The
+ * first call on a device looks the scratch's device address up with
+ * cudaGetSymbolAddress, so make that call before any stream capture.  All
+ * calls share the one array: calls that overlap on the GPU (other streams,
+ * other host threads) race and must not be issued. */
+#define GCLAW_NOALLOC_MAX_BLOCKS 131072
+int gclaw_step2_noalloc(const gclaw_solver *s, const double *qold_dev, double *qnew_dev,
+                        double dt, double *cfl_out, void *stream);
 
 #ifdef __cplusplus
 }
