@@ -110,13 +110,14 @@ def measured_peaks():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def profiled_traffic(kernel_tag):
-    """DRAM bytes per cell-update from the committed ncu summary, or None."""
+def profiled(kernel_tag, key):
+    """A per-cell-update figure (e.g. dram_bytes_per_cell_update) from the
+    committed ncu summary of a kernel, or None."""
     path = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.strip().startswith("dram_bytes_per_cell_update:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -306,7 +307,10 @@ def run_ours(args):
     t_kernel = secs / args.steps
     alg_bytes = 2 * m * 8 * cells
     achieved = alg_bytes / t_kernel * 1e-9
-    traffic_per_cell = profiled_traffic("step_fp64_shallow")
+    traffic_per_cell = profiled("step_fp64_shallow", "dram_bytes_per_cell_update")
+    fp64_inst = profiled("step_fp64_shallow", "fp64_inst_per_cell_update")
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    fp64_peak = 152 * 2 * sm_mhz * 1e6  # FP64 thread-instructions per second (2/clk/SM)
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -324,6 +328,11 @@ def run_ours(args):
                                  else round(traffic_per_cell * cells)),
                      "alg_bytes_per_launch": alg_bytes,
                      "note": "the FP64 step is bound by the FP64 pipe, not HBM"},
+        "roofline_fp64_pipe": (None if fp64_inst is None else {
+            "bound": "fp64 pipe", "inst_per_cell_update": fp64_inst,
+            "peak_inst_per_s": fp64_peak, "bound_gcell_updates_per_s": fp64_peak / fp64_inst * 1e-9,
+            "frac": round(value / world / (fp64_peak / fp64_inst * 1e-9), 4),
+            "source": "FP64 instruction count per cell-update from profiles/step_fp64_shallow.md"}),
         "clocks": clk,
         "gpu_launches": args.steps,
     }
@@ -335,12 +344,14 @@ def run_ours(args):
         q32 = dev32.q[c32.parity]
         err = float((q32 - q64).abs().sum() / q64.abs().sum())
         a32 = alg_bytes / (s32 / args.steps) * 1e-9
+        t32 = profiled("step_fp32_shallow", "dram_bytes_per_cell_update")
         out["fp32_bulk"] = {"value": round(v32, 4), "unit": UNIT, "dtype": "f32 fluxes, f64 q",
                             "rel_l1_vs_fp64": err, "speedup_vs_fp64": round(v32 / value, 3),
                             "ms_per_step": round(s32 / args.steps * 1e3, 4),
                             "roofline": {"bound": "hbm", "achieved": round(a32, 1),
                                          "peak": peak, "unit": "GB/s",
-                                         "frac": round(a32 / peak, 4)}}
+                                         "frac": round(a32 / peak, 4),
+                                         "traffic": None if t32 is None else round(t32 * cells)}}
         out["gpu_launches"] += args.steps
         del dev32
     # end to end through the C ABI with host buffers, every step

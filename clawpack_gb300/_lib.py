@@ -3,7 +3,9 @@ include/gclaw.h.
 
 The library must exist: there is no CPU fallback.  ``lib()`` raises
 ``RuntimeError`` when ``libgclaw.so`` has not been built
-(``python -c "import __graft_entry__ as g; g.build()"``).
+(``python -c "import __graft_entry__ as g; g.build()"``).  The environment
+variable GCLAW_LIBRARY, if set, names another build of the same sources to
+load instead (for example one compiled with different tile shapes).
 """
 from __future__ import annotations
 
@@ -111,7 +113,7 @@ _libs = {}
 def lib(strict=False):
     """Load libgclaw.so (or its -fmad=false twin) once and attach the C
     signatures."""
-    path = STRICT_LIB_PATH if strict else LIB_PATH
+    path = STRICT_LIB_PATH if strict else os.environ.get("GCLAW_LIBRARY", LIB_PATH)
     L = _libs.get(path)
     if L is None:
         if not os.path.exists(path):

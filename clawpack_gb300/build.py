@@ -35,9 +35,15 @@ def nvcc():
     raise RuntimeError("nvcc not found")
 
 
+# -prec-div/-prec-sqrt/-ftz only change single-precision arithmetic (the
+# FP32-bulk fluxes: approximate divide and square root, denormals flushed);
+# the FP64 step is compiled with IEEE divide and square root either way.
+FP32_FLAGS = ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
+
+
 def _cmd(out, extra):
     return [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-            f"-I{INCLUDE}", *extra, "-o", out, *SRC]
+            f"-I{INCLUDE}", *FP32_FLAGS, *extra, "-o", out, *SRC]
 
 
 def targets():

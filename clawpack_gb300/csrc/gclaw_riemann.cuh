@@ -22,6 +22,11 @@
 // Conventions: ql is the cell left of (below) the edge, qr the cell right of
 // (above) it.  W is [MW][M] row-major, s is [MW].  mu = IXY is the normal
 // momentum/velocity component, mv = 3 - IXY the transverse one.
+//
+// Per-cell quantities that every edge of a cell needs (square roots and
+// quotients of the cell state) are computed once per cell by cell_aux into
+// NA values and passed to rpn2 as al / ar; each is the same expression the
+// per-edge code evaluates, so the results are unchanged bit for bit.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -43,15 +48,18 @@ __device__ __forceinline__ float tmax<float>(float a, float b) { return fmaxf(a,
 // ---------------------------------------------------------------------------
 template <typename T>
 struct RpAcoustics {
-    static constexpr int M = 3, MW = 2, NR = 0;
+    static constexpr int M = 3, MW = 2, NR = 0, NA = 0;
     struct Params {
         T cc, zz;
     };
     static Params make(const double *pd) { return Params{(T)pd[2], (T)pd[3]}; }
 
+    __device__ __forceinline__ static void cell_aux(const Params &P, const T *q, T *aux) {}
+
     template <int IXY>
-    __device__ __forceinline__ static bool rpn2(const Params &P, const T *ql, const T *qr, T *W,
-                                                T *s, T *am, T *ap, T *R) {
+    __device__ __forceinline__ static bool rpn2(const Params &P, const T *ql, const T *qr,
+                                                const T *al, const T *ar, T *W, T *s, T *am,
+                                                T *ap, T *R) {
         constexpr int mu = IXY, mv = 3 - IXY;
         T d0 = qr[0] - ql[0];
         T d1 = qr[mu] - ql[mu];
@@ -102,45 +110,61 @@ __device__ __forceinline__ void split_sum(const T *sb, const T *wb, T *bm, T *bp
 // ---------------------------------------------------------------------------
 template <typename T>
 struct RpShallow {
-    static constexpr int M = 3, MW = 3, NR = 3;
+    static constexpr int M = 3, MW = 3, NR = 4, NA = 6;
     struct Params {
         T g;
         double gd;
     };
     static Params make(const double *pd) { return Params{(T)pd[0], pd[0]}; }
 
-    // Roe averages.  In FP32 bulk mode, depths below 1e-3 take the square
-    // roots and quotients in FP64 (near-dry states).
-    __device__ __forceinline__ static void roe(const Params &P, T hl, T hr, T hul, T hur, T hvl,
-                                               T hvr, T &u, T &v, T &c) {
+    // aux = (sqrt h, hu / sqrt h, hv / sqrt h, hu / h, hv / h, sqrt(g h))
+    __device__ __forceinline__ static void cell_aux(const Params &P, const T *q, T *aux) {
+        const T hs = sqrt(q[0]);
+        aux[0] = hs;
+        aux[1] = q[1] / hs;
+        aux[2] = q[2] / hs;
+        aux[3] = q[1] / q[0];
+        aux[4] = q[2] / q[0];
+        aux[5] = sqrt(P.g * q[0]);
+    }
+
+    // Roe state R = (ubar, vbar, cbar, 0.5 / cbar).  In FP32-bulk mode,
+    // depths below 1e-3 take the square roots and quotients in FP64
+    // (near-dry states).
+    template <int IXY>
+    __device__ __forceinline__ static void roe(const Params &P, const T *ql, const T *qr,
+                                               const T *al, const T *ar, T *R) {
+        constexpr int mu = IXY, mv = 3 - IXY;
+        const T hl = ql[0], hr = qr[0];
+        T u, v, c;
         if (sizeof(T) == 4 && (hl < (T)1e-3 || hr < (T)1e-3)) {
             double sl = sqrt((double)hl), sr = sqrt((double)hr), s2 = sl + sr;
-            u = (T)(((double)hul / sl + (double)hur / sr) / s2);
-            v = (T)(((double)hvl / sl + (double)hvr / sr) / s2);
+            u = (T)(((double)ql[mu] / sl + (double)qr[mu] / sr) / s2);
+            v = (T)(((double)ql[mv] / sl + (double)qr[mv] / sr) / s2);
             c = (T)sqrt(P.gd * (((double)hl + (double)hr) * 0.5));
-            return;
+        } else {
+            const T hsq2 = al[0] + ar[0];
+            u = (al[mu] + ar[mu]) / hsq2;
+            v = (al[mv] + ar[mv]) / hsq2;
+            const T hbar = (hl + hr) * (T)0.5;
+            c = sqrt(P.g * hbar);
         }
-        T hsqrtl = sqrt(hl), hsqrtr = sqrt(hr);
-        T hsq2 = hsqrtl + hsqrtr;
-        u = (hul / hsqrtl + hur / hsqrtr) / hsq2;
-        v = (hvl / hsqrtl + hvr / hsqrtr) / hsq2;
-        T hbar = (hl + hr) * (T)0.5;
-        c = sqrt(P.g * hbar);
+        R[0] = u; R[1] = v; R[2] = c; R[3] = (T)0.5 / c;
     }
 
     template <int IXY>
-    __device__ __forceinline__ static bool rpn2(const Params &P, const T *ql, const T *qr, T *W,
-                                                T *s, T *am, T *ap, T *R) {
+    __device__ __forceinline__ static bool rpn2(const Params &P, const T *ql, const T *qr,
+                                                const T *al, const T *ar, T *W, T *s, T *am,
+                                                T *ap, T *R) {
         constexpr int mu = IXY, mv = 3 - IXY;
         const T g = P.g;
-        T hl = ql[0], hr = qr[0];
-        T ubar, vbar, cbar;
-        roe(P, hl, hr, ql[mu], qr[mu], ql[mv], qr[mv], ubar, vbar, cbar);
-        R[0] = ubar; R[1] = vbar; R[2] = cbar;
+        const T hl = ql[0], hr = qr[0];
+        roe<IXY>(P, ql, qr, al, ar, R);
+        const T ubar = R[0], vbar = R[1], cbar = R[2], half = R[3];
         T d0 = hr - hl, d1 = qr[mu] - ql[mu], d2 = qr[mv] - ql[mv];
-        T a1 = ((ubar + cbar) * d0 - d1) * ((T)0.5 / cbar);
+        T a1 = ((ubar + cbar) * d0 - d1) * half;
         T a2 = -vbar * d0 + d2;
-        T a3 = (-(ubar - cbar) * d0 + d1) * ((T)0.5 / cbar);
+        T a3 = (-(ubar - cbar) * d0 + d1) * half;
         T *w1 = W, *w2 = W + 3, *w3 = W + 6;
         w1[0] = a1; w1[mu] = a1 * (ubar - cbar); w1[mv] = a1 * vbar;
         s[0] = ubar - cbar;
@@ -150,7 +174,7 @@ struct RpShallow {
         s[2] = ubar + cbar;
 
         // entropy fix: amdq first, apdq = sum(s W) - amdq
-        T s0 = ql[mu] / hl - sqrt(g * hl);
+        const T s0 = al[2 + mu] - al[5];  // u - c in the left cell
         if (s0 >= (T)0 && s[0] > (T)0) {
 #pragma unroll
             for (int k = 0; k < 3; k++) am[k] = (T)0;
@@ -170,7 +194,7 @@ struct RpShallow {
             if (s[1] < (T)0) {
 #pragma unroll
                 for (int k = 0; k < 3; k++) am[k] = am[k] + s[1] * w2[k];
-                T s03 = qr[mu] / hr + sqrt(g * hr);
+                const T s03 = ar[2 + mu] + ar[5];  // u + c in the right cell
                 T h3 = hr - w3[0];
                 T hu3 = qr[mu] - w3[mu];
                 T s3 = hu3 / h3 + sqrt(g * h3);
@@ -201,10 +225,10 @@ struct RpShallow {
     __device__ __forceinline__ static void rpt2(const Params &P, const T *R, const T *asdq, T *bm,
                                                 T *bp) {
         constexpr int mu = IXY, mv = 3 - IXY;
-        T ubar = R[0], vbar = R[1], cbar = R[2];
-        T a1 = ((vbar + cbar) * asdq[0] - asdq[mv]) * ((T)0.5 / cbar);
+        T ubar = R[0], vbar = R[1], cbar = R[2], half = R[3];
+        T a1 = ((vbar + cbar) * asdq[0] - asdq[mv]) * half;
         T a2 = asdq[mu] - ubar * asdq[0];
-        T a3 = (-(vbar - cbar) * asdq[0] + asdq[mv]) * ((T)0.5 / cbar);
+        T a3 = (-(vbar - cbar) * asdq[0] + asdq[mv]) * half;
         T wb[9], sb[3];
         wb[0] = a1; wb[mu] = a1 * ubar; wb[mv] = a1 * (vbar - cbar);
         sb[0] = vbar - cbar;
@@ -223,7 +247,7 @@ struct RpShallow {
 // ---------------------------------------------------------------------------
 template <typename T>
 struct RpEuler {
-    static constexpr int M = 4, MW = 4, NR = 7;
+    static constexpr int M = 4, MW = 4, NR = 7, NA = 8;
     struct Params {
         T gamma, gamma1;
         int efix;
@@ -236,13 +260,29 @@ struct RpEuler {
         return gamma1 * (q[3] - (T)0.5 * (q[1] * q[1] + q[2] * q[2]) / q[0]);
     }
 
+    // aux = (sqrt rho, p, rho u / sqrt rho, rho v / sqrt rho, (E + p) / sqrt rho,
+    //        u, v, c)
+    __device__ __forceinline__ static void cell_aux(const Params &P, const T *q, T *aux) {
+        const T rs = sqrt(q[0]);
+        const T p = pressure(P.gamma1, q);
+        aux[0] = rs;
+        aux[1] = p;
+        aux[2] = q[1] / rs;
+        aux[3] = q[2] / rs;
+        aux[4] = (q[3] + p) / rs;
+        aux[5] = q[1] / q[0];
+        aux[6] = q[2] / q[0];
+        aux[7] = sqrt(P.gamma * p / q[0]);
+    }
+
     template <int IXY>
-    __device__ __forceinline__ static bool rpn2(const Params &P, const T *ql, const T *qr, T *W,
-                                                T *s, T *am, T *ap, T *R) {
+    __device__ __forceinline__ static bool rpn2(const Params &P, const T *ql, const T *qr,
+                                                const T *al, const T *ar, T *W, T *s, T *am,
+                                                T *ap, T *R) {
         constexpr int mu = IXY, mv = 3 - IXY;
         const T gamma = P.gamma, gamma1 = P.gamma1;
-        T pl = pressure(gamma1, ql);
-        T pr = pressure(gamma1, qr);
+        const T pl = al[1];
+        const T pr = ar[1];
         T u, v, enth;
         if (sizeof(T) == 4 && (ql[0] < (T)1e-3 || qr[0] < (T)1e-3)) {
             // near-vacuum states: Roe averages in FP64
@@ -251,11 +291,10 @@ struct RpEuler {
             v = (T)(((double)ql[mv] / rl + (double)qr[mv] / rr) / rs);
             enth = (T)((((double)ql[3] + (double)pl) / rl + ((double)qr[3] + (double)pr) / rr) / rs);
         } else {
-            T rhsqrtl = sqrt(ql[0]), rhsqrtr = sqrt(qr[0]);
-            T rhsq2 = rhsqrtl + rhsqrtr;
-            u = (ql[mu] / rhsqrtl + qr[mu] / rhsqrtr) / rhsq2;
-            v = (ql[mv] / rhsqrtl + qr[mv] / rhsqrtr) / rhsq2;
-            enth = ((ql[3] + pl) / rhsqrtl + (qr[3] + pr) / rhsqrtr) / rhsq2;
+            const T rhsq2 = al[0] + ar[0];
+            u = (al[1 + mu] + ar[1 + mu]) / rhsq2;
+            v = (al[1 + mv] + ar[1 + mv]) / rhsq2;
+            enth = (al[4] + ar[4]) / rhsq2;
         }
         T u2v2 = u * u + v * v;
         T c2 = gamma1 * (enth - (T)0.5 * u2v2);
@@ -297,8 +336,7 @@ struct RpEuler {
             }
             return bad;
         }
-        T cim1 = sqrt(gamma * pl / ql[0]);
-        T s0 = ql[mu] / ql[0] - cim1;
+        const T s0 = al[4 + mu] - al[7];  // u - c in the left cell
         if (s0 >= (T)0 && s[0] > (T)0) {
 #pragma unroll
             for (int k = 0; k < 4; k++) am[k] = (T)0;
@@ -324,8 +362,7 @@ struct RpEuler {
                 for (int k = 0; k < 4; k++) am[k] = am[k] + s[1] * w2[k];
 #pragma unroll
                 for (int k = 0; k < 4; k++) am[k] = am[k] + s[2] * w3[k];
-                T ci = sqrt(gamma * pr / qr[0]);
-                T s3 = qr[mu] / qr[0] + ci;
+                const T s3 = ar[4 + mu] + ar[7];  // u + c in the right cell
                 T rho2 = qr[0] - w4[0];
                 T rhou2 = qr[mu] - w4[mu];
                 T rhov2 = qr[mv] - w4[mv];

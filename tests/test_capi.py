@@ -99,3 +99,19 @@ def test_shapes_versions_workspace():
         assert L.gclaw_strerror(st) and L.gclaw_strerror(st) != b"unknown status"
     s = good_solver(mx=100, my=50)
     assert L.gclaw_evolve_workspace_bytes(ctypes.byref(s)) >= 256 + 2 * 3 * 100 * 50 * 8
+
+
+def test_noalloc_refuses_oversized_grids_before_any_cuda_call():
+    """gclaw_step2_noalloc checks the grid against its static scratch first,
+    so the refusal needs no GPU (and no state buffers)."""
+    from tests.helpers import PD, SHAPES
+
+    L = _lib.lib()
+    for rp in (1, 2, 3):
+        for prec in (_lib.PREC_FP64, _lib.PREC_FP32_BULK):
+            s = make_solver_struct(rp, 16384, 16384, 1e-4, 1e-4, [3, 3], [3, 3],
+                                   [4] * SHAPES[rp][1], 2, 2, prec, PD[rp])
+            cfl = ctypes.c_double(-1.0)
+            assert L.gclaw_step2_noalloc(ctypes.byref(s), None, None, 1e-5, ctypes.byref(cfl),
+                                         None) == _lib.ERR_TOO_LARGE
+            assert cfl.value == -1.0

@@ -74,16 +74,17 @@ def test_noalloc_matches_step2_on_two_calls_in_a_row(oracle):
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch():
-    if not torch.cuda.is_available():
-        pytest.fail("GPU test run without a GPU")
+    """A grid beyond the scratch is refused before any launch.  The state
+    pointers are NULL, which the entry point would also refuse, so no kernel
+    can run on this call whatever the tile shape."""
     L = _lib.lib()
-    # 4096 x 8200 cells need 128 x 1025 FP64 thread blocks > 131072
-    s = make_solver_struct(2, 4096, 8200, 1e-3, 1e-3, [3, 3], [3, 3], [4, 4, 4], 2, 2,
-                           _lib.PREC_FP64, [1.0])
-    buf = torch.zeros(8, dtype=torch.float64, device="cuda")
-    cfl = ctypes.c_double(-1.0)
-    rc = L.gclaw_step2_noalloc(ctypes.byref(s), ctypes.c_void_p(buf.data_ptr()),
-                               ctypes.c_void_p(buf.data_ptr()), 1e-4, ctypes.byref(cfl), None)
-    assert rc == _lib.ERR_TOO_LARGE == -6
-    assert b"GCLAW_NOALLOC_MAX_BLOCKS" in L.gclaw_strerror(rc)
-    assert cfl.value == -1.0
+    # 16384^2 cells: at least 524288 thread blocks for every tile shape (<= 512 cells)
+    for rp, prec in ((2, _lib.PREC_FP64), (3, _lib.PREC_FP64), (2, _lib.PREC_FP32_BULK)):
+        mw = SHAPES[rp][1]
+        s = make_solver_struct(rp, 16384, 16384, 1e-4, 1e-4, [3, 3], [3, 3], [4] * mw, 2, 2,
+                               prec, PD[rp])
+        cfl = ctypes.c_double(-1.0)
+        rc = L.gclaw_step2_noalloc(ctypes.byref(s), None, None, 1e-5, ctypes.byref(cfl), None)
+        assert rc == _lib.ERR_TOO_LARGE == -6
+        assert cfl.value == -1.0
+    assert b"GCLAW_NOALLOC_MAX_BLOCKS" in L.gclaw_strerror(_lib.ERR_TOO_LARGE)
