@@ -55,6 +55,16 @@ class GclawSolver(ctypes.Structure):
     ]
 
 
+class GclawBatchProblem(ctypes.Structure):
+    _fields_ = [
+        ("mx", ctypes.c_int),
+        ("my", ctypes.c_int),
+        ("dx", ctypes.c_double),
+        ("dy", ctypes.c_double),
+        ("q_offset", ctypes.c_longlong),
+    ]
+
+
 class GclawCtrl(ctypes.Structure):
     _fields_ = [
         ("t", ctypes.c_double),
@@ -103,6 +113,10 @@ SIGNATURES = {
     "gclaw_step_host": (_I, [_SP, _P, _P, _D, _P, _SZ, ctypes.POINTER(_D), _P]),
     "gclaw_evolve_workspace_bytes": (_SZ, [_SP]),
     "gclaw_step2_noalloc": (_I, [_SP, _P, _P, _D, ctypes.POINTER(_D), _P]),
+    "gclaw_batch_table_bytes": (_SZ, [_I]),
+    "gclaw_batch_prepare": (_I, [_SP, _P, _I, _P, _SZ, ctypes.POINTER(_I), _P]),
+    "gclaw_batch_ctrl_init": (_I, [_P, _I, _P, _D, _D, _D, _D, _D, _I, _I, _I, _P]),
+    "gclaw_batch_advance": (_I, [_SP, _P, _I, _I, _P, _P, _P, _I, _P]),
     "gclaw_evolve_host": (_I, [_SP, _P, _P, _D, _D, _D, _I, _D, _D, _D, _I, _P, _SZ, _I,
                                ctypes.POINTER(GclawCtrl), _P]),
 }

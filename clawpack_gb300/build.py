@@ -8,7 +8,8 @@ Produces, next to this file:
   libgclaw_strict.so  the same sources with -fmad=false: every FP64 multiply
                       and add rounded separately, for bit-for-bit comparison
                       with the CPU oracle in the parity tests
-Both builds run in parallel; each is one translation unit.
+Every (library, source) pair compiles to an object in parallel under
+_build/, then each library is linked.
 """
 from __future__ import annotations
 
@@ -20,7 +21,8 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-SRC = [os.path.join(HERE, "csrc", "gclaw_step.cu")]
+SRC = [os.path.join(HERE, "csrc", "gclaw_step.cu"), os.path.join(HERE, "csrc", "gclaw_batch.cu")]
+BUILD_DIR = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -41,9 +43,9 @@ def nvcc():
 FP32_FLAGS = ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
 
 
-def _cmd(out, extra):
-    return [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-            f"-I{INCLUDE}", *FP32_FLAGS, *extra, "-o", out, *SRC]
+def _compile_cmd(src, obj, extra):
+    return [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            f"-I{INCLUDE}", *FP32_FLAGS, *extra, "-c", "-o", obj, src]
 
 
 def targets():
@@ -54,22 +56,32 @@ def targets():
 
 
 def build(verbose=False):
-    jobs = targets()
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    jobs = []
+    for out, extra in targets():
+        tag = os.path.splitext(os.path.basename(out))[0]
+        for src in SRC:
+            obj = os.path.join(BUILD_DIR, f"{tag}__{os.path.basename(src)}.o")
+            jobs.append((src, obj, extra))
 
-    def run(job):
-        out, extra = job
-        tmp = out + ".tmp"
-        cmd = _cmd(tmp, extra)
+    def run(cmd):
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            raise RuntimeError(f"nvcc failed for {out}:\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, out)
-        return out
+            raise RuntimeError(f"nvcc failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
 
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
-        return list(ex.map(run, jobs))
+        list(ex.map(lambda j: run(_compile_cmd(*j)), jobs))
+    built = []
+    for out, extra in targets():
+        tag = os.path.splitext(os.path.basename(out))[0]
+        objs = [os.path.join(BUILD_DIR, f"{tag}__{os.path.basename(src)}.o") for src in SRC]
+        tmp = out + ".tmp"
+        run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs])
+        os.replace(tmp, out)
+        built.append(out)
+    return built
 
 
 if __name__ == "__main__":

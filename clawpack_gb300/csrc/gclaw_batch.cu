@@ -1,0 +1,273 @@
+// gclaw_batch.cu -- many independent classic 2D problems advanced together.
+//
+// Thousands of problems of uneven grid sizes share one solver description
+// (Riemann solver, boundary conditions, limiters, precision) and have their
+// own grid, cell sizes and time-step control.  Their states live in two
+// large FP64 buffers (q0, q1), problem p at offset q_offset[p], each in the
+// (num_eqn, mx, my) Fortran layout of a single problem.
+//
+// One launch of batch_step_kernel is one attempted step of every unfinished
+// problem: a persistent grid (resident CTAs only) strides over a table of
+// all tiles of all problems; a CTA finds the problem of its tile by binary
+// search over the tiles' prefix sums, runs the same tile body as the
+// single-problem kernel (so each problem's result is bit-identical to
+// stepping it alone), and feeds the problem's CFL reduction.  The last tile
+// of a problem to finish applies PyClaw's evolve_to_time rules to that
+// problem's gclaw_ctrl (accept / reject, dt from its own CFL, stop after
+// max_accepted steps).  N steps are N launches, which capture into one CUDA
+// graph.  The table and the control blocks are caller-owned device memory.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "gclaw.h"
+#include "gclaw_step_impl.cuh"
+
+namespace gclaw {
+
+// One problem of the device table (48 bytes).
+struct BatchEntry {
+    int mx, my;
+    int tiles_x, ntiles;
+    double dx, dy;
+    long long q_off;
+    long long pad;
+};
+
+template <template <typename> class RPT, typename T, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1)
+    batch_step_kernel(const StepArgs base, const typename RPT<T>::Params P,
+                      const BatchEntry *__restrict__ ent, const int *__restrict__ tstart,
+                      int nprob, int total_tiles, double *q0, double *q1, gclaw_ctrl *ctrls) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double s_dt, s_dtdx, s_dtdy;
+    __shared__ int s_p, s_par, s_skip;
+    __shared__ T s_red[2][NT / 32];
+
+    for (int t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+        if (threadIdx.x == 0) {
+            int lo = 0, hi = nprob;  // largest p with tstart[p] <= t
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (__ldg(tstart + mid) <= t) lo = mid;
+                else hi = mid;
+            }
+            const volatile gclaw_ctrl *c = ctrls + lo;
+            const double dt = c->dt;
+            s_p = lo;
+            s_skip = c->done;
+            s_par = c->parity;
+            s_dt = dt;
+            s_dtdx = dt / ent[lo].dx;
+            s_dtdy = dt / ent[lo].dy;
+        }
+        __syncthreads();
+        if (!s_skip) {
+            const int p = s_p;
+            const BatchEntry e = ent[p];
+            StepArgs a = base;
+            a.mx = e.mx;
+            a.my = e.my;
+            a.dx = e.dx;
+            a.dy = e.dy;
+            double *qa = q0 + e.q_off, *qb = q1 + e.q_off;
+            const double *qin = s_par ? qb : qa;
+            double *qout = s_par ? qa : qb;
+            const int local = t - __ldg(tstart + p);
+            const int ti = local % e.tiles_x, tj = local / e.tiles_x;
+            const double dt = s_dt, dtdx = s_dtdx, dtdy = s_dtdy;
+            T smax_x = (T)0, smax_y = (T)0;
+            bool bad = false;
+            step_tile<RPT, T, TX, TY, NT>(a, P, qin, qout, dtdx, dtdy, ti * TX, tj * TY, smem_raw,
+                                          smax_x, smax_y, bad);
+            const int anybad = block_reduce<T, NT>(smax_x, smax_y, bad, s_red);
+            if (threadIdx.x == 0) {
+                gclaw_ctrl *c = ctrls + p;
+                atomicMax(&c->smax_bits[0], (unsigned long long)__double_as_longlong((double)smax_x));
+                atomicMax(&c->smax_bits[1], (unsigned long long)__double_as_longlong((double)smax_y));
+                if (anybad) atomicOr(&c->flags, 1u);
+                __threadfence();
+                if (atomicAdd(&c->blocks_done, 1u) == (unsigned)e.ntiles - 1u) {
+                    __threadfence();
+                    finish_step(c, 1, dt, dtdx, dtdy);
+                }
+            }
+        }
+        __syncthreads();  // shared memory is reused by the next tile
+    }
+}
+
+__global__ void batch_ctrl_init_kernel(gclaw_ctrl *c, int nprob, const double *dt0, double t,
+                                       double t_end, double cfl_max, double cfl_desired,
+                                       double dt_max, int max_steps, int max_accepted,
+                                       int dt_variable) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nprob) return;
+    double dt = dt0[p];
+    if (t + dt > t_end && t < t_end) dt = t_end - t;
+    if (t_end - t - dt < 1.0e-14 * t) dt = t_end - t;
+    gclaw_ctrl z;
+    memset(&z, 0, sizeof z);
+    z.t = t;
+    z.dt = dt;
+    z.t_start = t;
+    z.t_end = t_end;
+    z.cfl_max = cfl_max;
+    z.cfl_desired = cfl_desired;
+    z.dt_max = dt_max;
+    z.dtmin = dt;
+    z.dtmax = dt;
+    z.max_steps = max_steps;
+    z.max_accepted = max_accepted;
+    z.dt_variable = dt_variable;
+    z.done = (t >= t_end) ? 1 : 0;
+    z.status = GCLAW_OK;
+    c[p] = z;
+}
+
+template <template <typename> class RPT, typename T>
+static int launch_batch(const gclaw_solver *s, const StepArgs &a, const void *table, int nprob,
+                        int total_tiles, double *q0, double *q1, gclaw_ctrl *ctrls, int nlaunch,
+                        cudaStream_t st) {
+    using C = TileCfg<RPT, T>;
+    using RP = RPT<T>;
+    using TL = Tile<RP, C::TX, C::TY>;
+    constexpr size_t smem = TL::template smem_bytes<T>();
+    auto kern = batch_step_kernel<RPT, T, C::TX, C::TY, C::NT>;
+    static int grid_of_dev[64];  // persistent grid size per device, 0 = not yet set up
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return GCLAW_ERR_CUDA;
+    if (grid_of_dev[dev] == 0) {
+        int sms = 0, per_sm = 0;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::NT, smem) !=
+                cudaSuccess ||
+            per_sm < 1)
+            return GCLAW_ERR_CUDA;
+        grid_of_dev[dev] = sms * per_sm;
+    }
+    const int grid = total_tiles < grid_of_dev[dev] ? total_tiles : grid_of_dev[dev];
+    const BatchEntry *ent = (const BatchEntry *)table;
+    const int *tstart = (const int *)((const char *)table + sizeof(BatchEntry) * (size_t)nprob);
+    const typename RP::Params P = RP::make(s->problem_data);
+    for (int l = 0; l < nlaunch; l++)
+        kern<<<grid, C::NT, smem, st>>>(a, P, ent, tstart, nprob, total_tiles, q0, q1, ctrls);
+    return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
+}
+
+// gclaw_check on the shared part of a batch's solver description (the
+// per-problem grid fields are ignored).
+static int check_shared(const gclaw_solver *s) {
+    if (!s) return GCLAW_ERR_ARG;
+    gclaw_solver c = *s;
+    c.mx = c.my = 2;
+    c.dx = c.dy = 1.0;
+    return gclaw_check(&c);
+}
+
+}  // namespace gclaw
+
+using namespace gclaw;
+
+extern "C" {
+
+size_t gclaw_batch_table_bytes(int nprob) {
+    if (nprob < 1) return 0;
+    return sizeof(BatchEntry) * (size_t)nprob + sizeof(int) * ((size_t)nprob + 1);
+}
+
+int gclaw_batch_prepare(const gclaw_solver *s, const gclaw_batch_problem *probs, int nprob,
+                        void *table_dev, size_t table_bytes, int *total_tiles, void *stream) {
+    int rc = check_shared(s);
+    if (rc) return rc;
+    if (!probs || nprob < 1 || !table_dev || !total_tiles) return GCLAW_ERR_ARG;
+    if (table_bytes < gclaw_batch_table_bytes(nprob)) return GCLAW_ERR_WORKSPACE;
+    if (((uintptr_t)table_dev & 15u) != 0) return GCLAW_ERR_ARG;
+    int tx, ty;
+    tile_shape(s->rp, s->precision, &tx, &ty);
+    const size_t nbytes = gclaw_batch_table_bytes(nprob);
+    unsigned char *host = (unsigned char *)malloc(nbytes);
+    if (!host) return GCLAW_ERR_ARG;
+    BatchEntry *ent = (BatchEntry *)host;
+    int *tstart = (int *)(host + sizeof(BatchEntry) * (size_t)nprob);
+    long long tiles = 0;
+    for (int p = 0; p < nprob; p++) {
+        const gclaw_batch_problem &b = probs[p];
+        if (b.mx < 2 || b.my < 2 || !(b.dx > 0.0) || !(b.dy > 0.0) || b.q_offset < 0) {
+            free(host);
+            return GCLAW_ERR_ARG;
+        }
+        ent[p].mx = b.mx;
+        ent[p].my = b.my;
+        ent[p].tiles_x = (b.mx + tx - 1) / tx;
+        ent[p].ntiles = ent[p].tiles_x * ((b.my + ty - 1) / ty);
+        ent[p].dx = b.dx;
+        ent[p].dy = b.dy;
+        ent[p].q_off = b.q_offset;
+        ent[p].pad = 0;
+        tstart[p] = (int)tiles;
+        tiles += ent[p].ntiles;
+        if (tiles > 0x7fffffffll) {
+            free(host);
+            return GCLAW_ERR_ARG;
+        }
+    }
+    tstart[nprob] = (int)tiles;
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool ok = cudaMemcpyAsync(table_dev, host, nbytes, cudaMemcpyHostToDevice, st) ==
+                        cudaSuccess &&
+                    cudaStreamSynchronize(st) == cudaSuccess;
+    free(host);
+    if (!ok) return GCLAW_ERR_CUDA;
+    *total_tiles = (int)tiles;
+    return GCLAW_OK;
+}
+
+int gclaw_batch_ctrl_init(gclaw_ctrl *ctrls_dev, int nprob, const double *dt0_dev, double t,
+                          double t_end, double cfl_max, double cfl_desired, double dt_max,
+                          int max_steps, int max_accepted, int dt_variable, void *stream) {
+    if (!ctrls_dev || !dt0_dev || nprob < 1 || max_steps < 1) return GCLAW_ERR_ARG;
+    batch_ctrl_init_kernel<<<(nprob + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
+        ctrls_dev, nprob, dt0_dev, t, t_end, cfl_max, cfl_desired, dt_max, max_steps,
+        max_accepted, dt_variable ? 1 : 0);
+    return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
+}
+
+int gclaw_batch_advance(const gclaw_solver *s, const void *table_dev, int nprob, int total_tiles,
+                        double *q0_dev, double *q1_dev, gclaw_ctrl *ctrls_dev, int nlaunch,
+                        void *stream) {
+    int rc = check_shared(s);
+    if (rc) return rc;
+    if (!table_dev || nprob < 1 || total_tiles < 1 || !q0_dev || !q1_dev || !ctrls_dev ||
+        nlaunch < 0)
+        return GCLAW_ERR_ARG;
+    StepArgs a{};
+    a.ghosted = 0;
+    a.ctrl_mode = 1;
+    for (int d = 0; d < 2; d++) {
+        a.bc_lo[d] = s->bc_lower[d];
+        a.bc_hi[d] = s->bc_upper[d];
+    }
+    a.mthlim = 0;
+    for (int p = 0; p < 4; p++) a.mthlim |= (s->mthlim[p] & 0xff) << (8 * p);
+    a.order = s->order;
+    a.tw = s->transverse_waves;
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool f64 = s->precision == GCLAW_PREC_FP64;
+#define GCLAW_BATCH(RPT)                                                                         \
+    (f64 ? launch_batch<RPT, double>(s, a, table_dev, nprob, total_tiles, q0_dev, q1_dev,       \
+                                     ctrls_dev, nlaunch, st)                                     \
+         : launch_batch<RPT, float>(s, a, table_dev, nprob, total_tiles, q0_dev, q1_dev,        \
+                                    ctrls_dev, nlaunch, st))
+    switch (s->rp) {
+    case GCLAW_RP_ACOUSTICS_2D: return GCLAW_BATCH(RpAcoustics);
+    case GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D: return GCLAW_BATCH(RpShallow);
+    default: return GCLAW_BATCH(RpEuler);
+    }
+#undef GCLAW_BATCH
+}
+
+}  // extern "C"

@@ -1,0 +1,587 @@
+// gclaw_step_impl.cuh -- device code shared by the single-problem step
+// (gclaw_step.cu) and the batched step (gclaw_batch.cu): tile shapes, the
+// phases of one tile of the classic unsplit step, the tile body step_tile,
+// block reductions and the evolve_to_time rules applied by the last block.
+// See gclaw_step.cu for the description of the phases.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gclaw.h"
+#include "gclaw_riemann.cuh"
+
+namespace gclaw {
+
+struct StepArgs {
+    const double *qin[2];
+    double *qout[2];
+    gclaw_ctrl *ctrl;
+    double dt, dx, dy;
+    int mx, my;
+    int ghosted;   // input is a ghost-filled qbc (mx+4, my+4); output written at +2 offset
+    int ctrl_mode; // dt / parity / done from ctrl; evolve rules in the last block
+    int bc_lo[2], bc_hi[2];
+    int mthlim;  // limiter id of wave p in bits 8p..8p+7
+    int order, tw;
+};
+
+// Value of component k of qbc(gi, gj) for gi in [-2, mx+1], gj in [-2, my+1]
+// (coordinates outside are clamped; the tile's cells past the domain only
+// feed edges whose results are discarded).
+template <int M>
+__device__ __forceinline__ double load_q(const StepArgs &a, const double *__restrict__ q, int k,
+                                         int gi, int gj) {
+    gi = min(max(gi, -2), a.mx + 1);
+    gj = min(max(gj, -2), a.my + 1);
+    if (a.ghosted)
+        return __ldg(q + k + (size_t)M * ((size_t)(gi + 2) + (size_t)(a.mx + 4) * (size_t)(gj + 2)));
+    bool neg = false;
+    int sj = gj;
+    if (gj < 0) {
+        int b = a.bc_lo[1];
+        if (b == GCLAW_BC_EXTRAP) sj = 0;
+        else if (b == GCLAW_BC_PERIODIC) sj = gj + a.my;
+        else { sj = -1 - gj; neg = (k == 2); }
+    } else if (gj >= a.my) {
+        int b = a.bc_hi[1];
+        if (b == GCLAW_BC_EXTRAP) sj = a.my - 1;
+        else if (b == GCLAW_BC_PERIODIC) sj = gj - a.my;
+        else { sj = 2 * a.my - 1 - gj; neg = (k == 2); }
+    }
+    int si = gi;
+    if (gi < 0) {
+        int b = a.bc_lo[0];
+        if (b == GCLAW_BC_EXTRAP) si = 0;
+        else if (b == GCLAW_BC_PERIODIC) si = gi + a.mx;
+        else { si = -1 - gi; neg = neg || (k == 1); }
+    } else if (gi >= a.mx) {
+        int b = a.bc_hi[0];
+        if (b == GCLAW_BC_EXTRAP) si = a.mx - 1;
+        else if (b == GCLAW_BC_PERIODIC) si = gi - a.mx;
+        else { si = 2 * a.mx - 1 - gi; neg = neg || (k == 1); }
+    }
+    double v = __ldg(q + k + (size_t)M * ((size_t)si + (size_t)a.mx * (size_t)sj));
+    return neg ? -v : v;
+}
+
+// Exact double <-> float conversions done with integer operations.  On
+// GB300 the conversion instructions issue to the FP64 pipe, which is the
+// scarce unit; these give the same bits as __double2float_rn and the float
+// to double widening for zeros and normal numbers and fall back to the
+// instructions otherwise (denormals, very small or large magnitudes,
+// infinities, NaN).
+__device__ __forceinline__ float d2f_rn_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);  // +-0
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    if (e - 897u < 253u) {  // float exponent 1..253
+        unsigned f = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+        const unsigned rem = lo & 0x1fffffffu;
+        f += (rem > 0x10000000u) | ((rem == 0x10000000u) & f);  // round to nearest even
+        return __uint_as_float((hi & 0x80000000u) | f);
+    }
+    return __double2float_rn(x);
+}
+
+__device__ __forceinline__ double f2d_bits(float x) {
+    const unsigned u = __float_as_uint(x);
+    if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);  // +-0
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e - 1u < 254u)  // normal
+        return __hiloint2double(
+            (int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3)),
+            (int)(u << 29));
+    return (double)x;
+}
+
+template <typename T>
+__device__ __forceinline__ T from_double(double v);
+template <>
+__device__ __forceinline__ double from_double<double>(double v) { return v; }
+template <>
+__device__ __forceinline__ float from_double<float>(double v) { return d2f_rn_bits(v); }
+
+// Edge indexing of one sweep.  The x-sweep's edges sit on a (TX+3) x (TY+2)
+// grid (slices are rows), the y-sweep's on a (TX+2) x (TY+3) grid (slices are
+// columns).  Both are stored x-fastest, so consecutive threads touch
+// consecutive x positions and shared-memory accesses are conflict-free.
+//   phase 1: all edges, (ea along the slice, sl)
+//   phase 2: the limited edges, (e2 = ea - 1, sl)
+template <int IXY, int TX, int TY>
+struct SweepIdx {
+    static constexpr int NA = IXY == 1 ? TX + 3 : TY + 3;  // edges along a slice
+    static constexpr int NS = IXY == 1 ? TY + 2 : TX + 2;  // slices
+    static constexpr int NA2 = NA - 2;                      // limited edges per slice
+    static constexpr int STEP1 = IXY == 1 ? 1 : NS;         // next edge along the sweep, phase 1
+    static constexpr int STEP2 = IXY == 1 ? 1 : NS;         // next edge along the sweep, phase 2
+    __device__ __forceinline__ static int item1(int ea, int sl) {
+        return IXY == 1 ? sl * NA + ea : ea * NS + sl;
+    }
+    __device__ __forceinline__ static void split1(int it, int &ea, int &sl) {
+        if (IXY == 1) { ea = it % NA; sl = it / NA; }
+        else { sl = it % NS; ea = it / NS; }
+    }
+    __device__ __forceinline__ static int item2(int e2, int sl) {
+        return IXY == 1 ? sl * NA2 + e2 : e2 * NS + sl;
+    }
+    __device__ __forceinline__ static void split2(int it, int &e2, int &sl) {
+        if (IXY == 1) { e2 = it % NA2; sl = it / NA2; }
+        else { sl = it % NS; e2 = it / NS; }
+    }
+};
+
+// Tile shape (cells per CTA in x and y, threads per CTA) per solver and
+// precision, chosen by measurement on GB300 (2048^2 runs): larger tiles
+// recompute fewer halo edges, which matters most for the FP64 kernels
+// (FP64-pipe bound); the FP64 Euler tile is smaller because its per-edge
+// records (35 doubles) must fit in shared memory.  GCLAW_TILE_F32_{TX,TY,NT}
+// and GCLAW_TILE_F64_{TX,TY,NT} override every solver at build time (sweeps).
+template <template <typename> class RPT, typename T>
+struct TileCfg;
+#define GCLAW_TILE_CFG(RPT, T, tx, ty, nt)                           \
+    template <>                                                       \
+    struct TileCfg<RPT, T> {                                          \
+        static constexpr int TX = tx, TY = ty, NT = nt;               \
+    };
+#if defined(GCLAW_TILE_F64_TX)
+GCLAW_TILE_CFG(RpAcoustics, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_TILE_F64_NT)
+GCLAW_TILE_CFG(RpShallow, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_TILE_F64_NT)
+GCLAW_TILE_CFG(RpEuler, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_TILE_F64_NT)
+#else
+GCLAW_TILE_CFG(RpAcoustics, double, 32, 16, 256)
+GCLAW_TILE_CFG(RpShallow, double, 32, 16, 256)
+GCLAW_TILE_CFG(RpEuler, double, 16, 16, 256)
+#endif
+#if defined(GCLAW_TILE_F32_TX)
+GCLAW_TILE_CFG(RpAcoustics, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_TILE_F32_NT)
+GCLAW_TILE_CFG(RpShallow, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_TILE_F32_NT)
+GCLAW_TILE_CFG(RpEuler, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_TILE_F32_NT)
+#else
+GCLAW_TILE_CFG(RpAcoustics, float, 32, 16, 512)
+GCLAW_TILE_CFG(RpShallow, float, 32, 16, 512)
+GCLAW_TILE_CFG(RpEuler, float, 24, 16, 384)
+#endif
+#undef GCLAW_TILE_CFG
+
+// Cells per CTA of the kernel that runs solver rp at the given precision.
+static inline void tile_shape(int rp, int precision, int *tx, int *ty) {
+    const bool f64 = precision == GCLAW_PREC_FP64;
+    switch (rp) {
+    case GCLAW_RP_ACOUSTICS_2D:
+        *tx = f64 ? TileCfg<RpAcoustics, double>::TX : TileCfg<RpAcoustics, float>::TX;
+        *ty = f64 ? TileCfg<RpAcoustics, double>::TY : TileCfg<RpAcoustics, float>::TY;
+        return;
+    case GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D:
+        *tx = f64 ? TileCfg<RpShallow, double>::TX : TileCfg<RpShallow, float>::TX;
+        *ty = f64 ? TileCfg<RpShallow, double>::TY : TileCfg<RpShallow, float>::TY;
+        return;
+    default:
+        *tx = f64 ? TileCfg<RpEuler, double>::TX : TileCfg<RpEuler, float>::TX;
+        *ty = f64 ? TileCfg<RpEuler, double>::TY : TileCfg<RpEuler, float>::TY;
+        return;
+    }
+}
+
+template <class RP, int TX, int TY>
+struct Tile {
+    static constexpr int M = RP::M, MW = RP::MW, NR = RP::NR, NA = RP::NA;
+    // shared-memory row stride: TX+4 cells plus one pad column so that the
+    // stride is odd and column-wise (y-sweep) reads hit distinct banks
+    static constexpr int QW = TX + 5, QH = TY + 4, QN = QW * QH;
+    static constexpr int NE1X = (TX + 3) * (TY + 2), NE1Y = (TX + 2) * (TY + 3);
+    static constexpr int NE1 = NE1X > NE1Y ? NE1X : NE1Y;
+    static constexpr int NE2X = (TX + 1) * (TY + 2), NE2Y = (TX + 2) * (TY + 1);
+    static constexpr int NE2 = NE2X > NE2Y ? NE2X : NE2Y;
+    // edge area fields: W[MW*M], s[MW], amdq[M], apdq[M], Roe state[NR]
+    static constexpr int FW = 0, FS = MW * M, FAM = FS + MW, FAP = FAM + M, FR = FAP + M;
+    static constexpr int EAW = FR + NR;
+    // second-phase fields: fadd, B-A-, B+A-, B-A+, B+A+ (each M)
+    static constexpr int GFA = 0, GMM = M, GPM = 2 * M, GMP = 3 * M, GPP = 4 * M, EBW = 5 * M;
+    // the per-cell aux values of a sweep live in the second-phase area,
+    // which is free while the sweep's Riemann problems are solved
+    static_assert(NA * QN <= EBW * NE2, "cell aux area does not fit");
+    template <typename T>
+    static constexpr size_t smem_bytes() {
+        return sizeof(T) * ((size_t)M * QN + (size_t)EAW * NE1 + (size_t)EBW * NE2);
+    }
+};
+
+// ---- phase 0: per-cell square roots and quotients for one sweep ---------
+template <class RP, typename T, int IXY, int TX, int TY, int NT>
+__device__ __forceinline__ void phase_aux(const typename RP::Params &P, const T *QS, T *CA) {
+    using TL = Tile<RP, TX, TY>;
+    constexpr int M = RP::M, NA = RP::NA;
+    if (NA == 0) return;
+    // cells the sweep's edges touch: x-sweep cx 0..TX+3, cy 1..TY+2;
+    // y-sweep cx 1..TX+2, cy 0..TY+3
+    constexpr int W = (IXY == 1) ? TX + 4 : TX + 2, H = (IXY == 1) ? TY + 2 : TY + 4;
+    constexpr int X0 = (IXY == 1) ? 0 : 1, Y0 = (IXY == 1) ? 1 : 0;
+    for (int it = threadIdx.x; it < W * H; it += NT) {
+        const int c = (Y0 + it / W) * TL::QW + X0 + it % W;
+        T q[M], aux[NA > 0 ? NA : 1];
+#pragma unroll
+        for (int k = 0; k < M; k++) q[k] = QS[k * TL::QN + c];
+        RP::cell_aux(P, q, aux);
+#pragma unroll
+        for (int f = 0; f < NA; f++) CA[f * TL::QN + c] = aux[f];
+    }
+}
+
+// ---- phase 1: normal Riemann problems on every edge of the sweep ---------
+template <class RP, typename T, int IXY, int TX, int TY, int NT>
+__device__ __forceinline__ void phase_rpn2(const typename RP::Params &P, const T *QS, const T *CA,
+                                           T *EA, int i0, int j0, int mx, int my, T &smax,
+                                           bool &bad) {
+    using TL = Tile<RP, TX, TY>;
+    constexpr int M = RP::M, MW = RP::MW, NR = RP::NR, NA = RP::NA;
+    using SI = SweepIdx<IXY, TX, TY>;
+    constexpr int NA1 = SI::NA, NS = SI::NS;
+    const int gbase_e = ((IXY == 1) ? i0 : j0) - 1;
+    const int gbase_s = ((IXY == 1) ? j0 : i0) - 1;
+    const int n = (IXY == 1) ? mx : my, nt = (IXY == 1) ? my : mx;
+    for (int it = threadIdx.x; it < NA1 * NS; it += NT) {
+        int ea, sl;
+        SI::split1(it, ea, sl);
+        // left / lower cell and the step to the right / upper cell
+        const int cl = (IXY == 1) ? (sl + 1) * TL::QW + ea : ea * TL::QW + sl + 1;
+        const int cr = cl + ((IXY == 1) ? 1 : TL::QW);
+        T ql[M], qr[M], al[NA > 0 ? NA : 1], ar[NA > 0 ? NA : 1];
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            ql[k] = QS[k * TL::QN + cl];
+            qr[k] = QS[k * TL::QN + cr];
+        }
+#pragma unroll
+        for (int f = 0; f < NA; f++) {
+            al[f] = CA[f * TL::QN + cl];
+            ar[f] = CA[f * TL::QN + cr];
+        }
+        T W[MW * M], s[MW], am[M], ap[M], R[NR > 0 ? NR : 1];
+        bad |= RP::template rpn2<IXY>(P, ql, qr, al, ar, W, s, am, ap, R);
+#pragma unroll
+        for (int f = 0; f < MW * M; f++) EA[(TL::FW + f) * TL::NE1 + it] = W[f];
+#pragma unroll
+        for (int p = 0; p < MW; p++) EA[(TL::FS + p) * TL::NE1 + it] = s[p];
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            EA[(TL::FAM + k) * TL::NE1 + it] = am[k];
+            EA[(TL::FAP + k) * TL::NE1 + it] = ap[k];
+        }
+#pragma unroll
+        for (int r = 0; r < NR; r++) EA[(TL::FR + r) * TL::NE1 + it] = R[r];
+        const int ge = gbase_e + ea, gs = gbase_s + sl;
+        if (ea >= 1 && ea <= NA1 - 2 && ge <= n && gs <= nt) {
+#pragma unroll
+            for (int p = 0; p < MW; p++) {
+                bad |= (s[p] != s[p]);
+                smax = tmax(smax, (T)fabs(s[p]));
+            }
+        }
+    }
+}
+
+// ---- phase 2: limiter, correction flux, transverse splitting -------------
+template <class RP, typename T, int IXY, int TX, int TY, int NT>
+__device__ __forceinline__ void phase_limit(const typename RP::Params &P, const T *EA, T *EB,
+                                            int mthlim, int order, int tw, T dtdn) {
+    using TL = Tile<RP, TX, TY>;
+    constexpr int M = RP::M, MW = RP::MW, NR = RP::NR;
+    using SI = SweepIdx<IXY, TX, TY>;
+    constexpr int NS = SI::NS, NA2 = SI::NA2, STEP = SI::STEP1;
+    for (int it = threadIdx.x; it < NA2 * NS; it += NT) {
+        int e2, sl;
+        SI::split2(it, e2, sl);
+        const int ie = SI::item1(e2 + 1, sl);
+        T W[MW * M], s[MW], am[M], ap[M], cq[M];
+#pragma unroll
+        for (int f = 0; f < MW * M; f++) W[f] = EA[(TL::FW + f) * TL::NE1 + ie];
+#pragma unroll
+        for (int p = 0; p < MW; p++) s[p] = EA[(TL::FS + p) * TL::NE1 + ie];
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            am[k] = EA[(TL::FAM + k) * TL::NE1 + ie];
+            ap[k] = EA[(TL::FAP + k) * TL::NE1 + ie];
+            cq[k] = (T)0;
+        }
+        if (order == 2) {
+#pragma unroll
+            for (int p = 0; p < MW; p++) {
+                const int lim = (mthlim >> (8 * p)) & 0xff;
+                if (lim == 0) continue;
+                T wn2 = (T)0;
+#pragma unroll
+                for (int k = 0; k < M; k++) wn2 = wn2 + W[p * M + k] * W[p * M + k];
+                if (wn2 == (T)0) continue;
+                T dot = (T)0;
+                if (s[p] > (T)0) {
+#pragma unroll
+                    for (int k = 0; k < M; k++)
+                        dot = dot + EA[(TL::FW + p * M + k) * TL::NE1 + ie - STEP] * W[p * M + k];
+                } else {
+#pragma unroll
+                    for (int k = 0; k < M; k++)
+                        dot = dot + W[p * M + k] * EA[(TL::FW + p * M + k) * TL::NE1 + ie + STEP];
+                }
+                const T phi = philim<T>(lim, dot / wn2);
+#pragma unroll
+                for (int k = 0; k < M; k++) W[p * M + k] = phi * W[p * M + k];
+            }
+            const T dtave = (T)0.5 * (dtdn + dtdn);
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                T c = (T)0;
+#pragma unroll
+                for (int p = 0; p < MW; p++) {
+                    const T sa = fabs(s[p]);
+                    c = c + sa * ((T)1 - sa * dtave) * W[p * M + k];
+                }
+                cq[k] = c;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < M; k++) EB[(TL::GFA + k) * TL::NE2 + it] = (T)0 + (T)0.5 * cq[k];
+        T bmm[M], bpm[M], bmp[M], bpp[M];
+        if (tw > 0) {
+            if (order == 2 && tw == 2) {
+#pragma unroll
+                for (int k = 0; k < M; k++) {
+                    am[k] = am[k] + cq[k];
+                    ap[k] = ap[k] - cq[k];
+                }
+            }
+            T R[NR > 0 ? NR : 1];
+#pragma unroll
+            for (int r = 0; r < NR; r++) R[r] = EA[(TL::FR + r) * TL::NE1 + ie];
+            RP::template rpt2<IXY>(P, R, am, bmm, bpm);
+            RP::template rpt2<IXY>(P, R, ap, bmp, bpp);
+        } else {
+#pragma unroll
+            for (int k = 0; k < M; k++) bmm[k] = bpm[k] = bmp[k] = bpp[k] = (T)0;
+        }
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            EB[(TL::GMM + k) * TL::NE2 + it] = bmm[k];
+            EB[(TL::GPM + k) * TL::NE2 + it] = bpm[k];
+            EB[(TL::GMP + k) * TL::NE2 + it] = bmp[k];
+            EB[(TL::GPP + k) * TL::NE2 + it] = bpp[k];
+        }
+    }
+}
+
+// ---- phase 3: ordered per-cell accumulation of one sweep ------------------
+// acc starts at q (FP64 mode) or 0 (FP32 mode) and receives, in order, the
+// slice-before term, the own-slice term and the slice-after term.
+template <class RP, typename T, typename A, int IXY, int TX, int TY, int NT, int NC>
+__device__ __forceinline__ void phase_accum(const T *EA, const T *EB, A (*acc)[RP::M], T dtdn,
+                                            T dtdt) {
+    using TL = Tile<RP, TX, TY>;
+    constexpr int M = RP::M;
+    using SI = SweepIdx<IXY, TX, TY>;
+    constexpr int S1 = SI::STEP1, S2 = SI::STEP2;
+    const T h = (T)0.5 * dtdn;
+#pragma unroll
+    for (int t = 0; t < NC; t++) {
+        const int n = threadIdx.x + t * NT;
+        if (n >= TX * TY) break;
+        const int ci = n % TX, cj = n / TX;
+        const int al = (IXY == 1) ? ci : cj;   // position along the sweep
+        const int so = ((IXY == 1) ? cj : ci) + 1;  // own slice
+        // left / right edge of the cell in the phase-1 area, and in the
+        // phase-2 area for the slice before, the own slice and the slice after
+        const int el = SI::item1(al + 1, so), er = el + S1;
+        const int b0 = SI::item2(al, so - 1), o0 = SI::item2(al, so), a0 = SI::item2(al, so + 1);
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            const T *BMM = EB + (TL::GMM + k) * TL::NE2, *BPM = EB + (TL::GPM + k) * TL::NE2;
+            const T *BMP = EB + (TL::GMP + k) * TL::NE2, *BPP = EB + (TL::GPP + k) * TL::NE2;
+            const T *FA = EB + (TL::GFA + k) * TL::NE2;
+            const T g2b = ((T)0 - h * BPM[b0 + S2]) - h * BPP[b0];
+            const T qo = ((T)0 - dtdn * EA[(TL::FAP + k) * TL::NE1 + el]) -
+                         dtdn * EA[(TL::FAM + k) * TL::NE1 + er];
+            const T fo = FA[o0 + S2] - FA[o0];
+            const T g1o = ((T)0 - h * BMM[o0 + S2]) - h * BMP[o0];
+            const T g2o = ((T)0 - h * BPM[o0 + S2]) - h * BPP[o0];
+            const T g1a = ((T)0 - h * BMM[a0 + S2]) - h * BMP[a0];
+            A v = acc[t][k];
+            v = v + (A)dtdt * (A)g2b;
+            v = v + (A)qo - (A)dtdn * (A)fo - (A)dtdt * ((A)g2o - (A)g1o);
+            v = v - (A)dtdt * (A)g1a;
+            acc[t][k] = v;
+        }
+    }
+}
+
+// ---- last block: CFL and the evolve_to_time rules --------------------------
+static __device__ void finish_step(gclaw_ctrl *c, int ctrl_mode, double dt, double dtdx,
+                                   double dtdy) {
+    const double sx = __longlong_as_double((long long)atomicExch(&c->smax_bits[0], 0ull));
+    const double sy = __longlong_as_double((long long)atomicExch(&c->smax_bits[1], 0ull));
+    const unsigned flags = atomicExch(&c->flags, 0u);
+    const double cx = dtdx * sx, cy = dtdy * sy;
+    const double cfl = cx > cy ? cx : cy;
+    c->cfl = cfl;
+    c->blocks_done = 0u;
+    if (!ctrl_mode) {
+        c->status = flags ? GCLAW_NONPHYSICAL : GCLAW_OK;
+        return;
+    }
+    c->attempts += 1;
+    if (flags) {
+        c->status = GCLAW_NONPHYSICAL;
+        c->done = 1;
+        return;
+    }
+    const bool accept = cfl <= c->cfl_max;
+    if (accept) {
+        c->cflmax = fmax(cfl, c->cflmax);
+        c->numsteps += 1;
+        if (c->dt_variable) c->t = c->t + dt;
+        else c->t = c->t_start + (double)c->numsteps * dt;
+        c->parity ^= 1;
+    } else if (!c->dt_variable) {
+        c->status = GCLAW_CFL_FIXED_DT;
+        c->done = 1;
+        return;
+    }
+    if (c->t >= c->t_end || (c->max_accepted >= 0 && c->numsteps >= c->max_accepted)) {
+        c->done = 1;
+        return;
+    }
+    if (c->attempts >= c->max_steps) {
+        c->status = GCLAW_MAX_STEPS;
+        c->done = 1;
+        return;
+    }
+    if (c->dt_variable) {
+        double ndt;
+        if (cfl > 0.0) {
+            ndt = fmin(c->dt_max, dt * c->cfl_desired / cfl);
+            c->dtmin = fmin(ndt, c->dtmin);
+            c->dtmax = fmax(ndt, c->dtmax);
+        } else {
+            ndt = c->dt_max;
+        }
+        if (c->t + ndt > c->t_end && c->t_start < c->t_end) ndt = c->t_end - c->t;
+        if (c->t_end - c->t - ndt < 1.0e-14 * c->t) ndt = c->t_end - c->t;
+        c->dt = ndt;
+    }
+}
+
+// ---- one tile, both sweeps --------------------------------------------------
+// Runs the whole step for the tile at (i0, j0): load with boundary
+// conditions, both sweeps, and the write of the new state.  Returns the
+// tile's max |s| on x- and y-edges and whether a Riemann problem met a
+// non-physical state.  dtdx and dtdy are the block's shared copies.
+template <template <typename> class RPT, typename T, int TX, int TY, int NT>
+__device__ __forceinline__ void step_tile(const StepArgs &a, const typename RPT<T>::Params &P,
+                                          const double *__restrict__ qin,
+                                          double *__restrict__ qout, double dtdx, double dtdy,
+                                          int i0, int j0, unsigned char *smem_raw, T &smax_x,
+                                          T &smax_y, bool &bad) {
+    using RP = RPT<T>;
+    using TL = Tile<RP, TX, TY>;
+    using A = T;  // FP64: accumulate q itself; FP32: accumulate the increment
+    constexpr int M = RP::M;
+    constexpr int NC = (TX * TY + NT - 1) / NT;
+    constexpr bool FP64 = sizeof(T) == 8;
+    T *QS = reinterpret_cast<T *>(smem_raw);
+    T *EA = QS + M * TL::QN;
+    T *EB = EA + TL::EAW * TL::NE1;
+    T *CA = EB;
+    const T tdtdx = (T)dtdx, tdtdy = (T)dtdy;
+
+    // L: tile + halo.  When the whole window lies inside the input array
+    // (every tile but the boundary ones) it is read row by row with
+    // coalesced loads; otherwise each value goes through the boundary
+    // conditions (load_q).
+    const int off = a.ghosted ? 2 : 0, nx = a.mx + 2 * off, ny = a.my + 2 * off;
+    const bool inside = i0 - 2 + off >= 0 && i0 + TX + 2 + off <= nx && j0 - 2 + off >= 0 &&
+                        j0 + TY + 2 + off <= ny;
+    if (inside) {
+        constexpr int RW = (TX + 4) * M;  // doubles per tile row
+        const double *__restrict__ base =
+            qin + (size_t)M * ((size_t)(i0 - 2 + off) + (size_t)nx * (size_t)(j0 - 2 + off));
+        const size_t rs = (size_t)M * (size_t)nx;
+        for (int idx = threadIdx.x; idx < RW * TL::QH; idx += NT) {
+            const int r = idx / RW, c = idx - r * RW;
+            const int cell = c / M, k = c - cell * M;
+            QS[k * TL::QN + r * TL::QW + cell] = from_double<T>(__ldg(base + r * rs + c));
+        }
+    } else {
+        for (int idx = threadIdx.x; idx < (TX + 4) * TL::QH * M; idx += NT) {
+            const int k = idx % M, cell = idx / M;
+            const int cx = cell % (TX + 4), cy = cell / (TX + 4);
+            QS[k * TL::QN + cy * TL::QW + cx] =
+                from_double<T>(load_q<M>(a, qin, k, i0 - 2 + cx, j0 - 2 + cy));
+        }
+    }
+    __syncthreads();
+
+    A acc[NC][M];
+#pragma unroll
+    for (int t = 0; t < NC; t++) {
+        const int n = threadIdx.x + t * NT;
+        const int ci = n % TX, cj = n / TX;
+#pragma unroll
+        for (int k = 0; k < M; k++)
+            acc[t][k] = (FP64 && n < TX * TY) ? QS[k * TL::QN + (cj + 2) * TL::QW + ci + 2] : (A)0;
+    }
+
+    phase_aux<RP, T, 1, TX, TY, NT>(P, QS, CA);
+    __syncthreads();
+    phase_rpn2<RP, T, 1, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, smax_x, bad);
+    __syncthreads();
+    phase_limit<RP, T, 1, TX, TY, NT>(P, EA, EB, a.mthlim, a.order, a.tw, tdtdx);
+    __syncthreads();
+    phase_accum<RP, T, A, 1, TX, TY, NT, NC>(EA, EB, acc, tdtdx, tdtdy);
+    __syncthreads();
+    phase_aux<RP, T, 2, TX, TY, NT>(P, QS, CA);
+    __syncthreads();
+    phase_rpn2<RP, T, 2, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, smax_y, bad);
+    __syncthreads();
+    phase_limit<RP, T, 2, TX, TY, NT>(P, EA, EB, a.mthlim, a.order, a.tw, tdtdy);
+    __syncthreads();
+    phase_accum<RP, T, A, 2, TX, TY, NT, NC>(EA, EB, acc, tdtdy, tdtdx);
+
+    const int onx = a.ghosted ? a.mx + 4 : a.mx, ooff = a.ghosted ? 2 : 0;
+#pragma unroll
+    for (int t = 0; t < NC; t++) {
+        const int n = threadIdx.x + t * NT;
+        if (n >= TX * TY) break;
+        const int gi = i0 + n % TX, gj = j0 + n / TX;
+        if (gi < a.mx && gj < a.my) {
+            const size_t o = (size_t)M * ((size_t)(gi + ooff) + (size_t)onx * (size_t)(gj + ooff));
+#pragma unroll
+            for (int k = 0; k < M; k++)
+                qout[o + k] = FP64 ? (double)acc[t][k] : __ldg(qin + o + k) + f2d_bits((float)acc[t][k]);
+        }
+    }
+}
+
+// Block-wide max of two values of type T (result valid in thread 0) and OR
+// of a flag (valid in every thread).
+template <typename T, int NT>
+__device__ __forceinline__ int block_reduce(T &x, T &y, bool flag, T (*red)[NT / 32]) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        x = tmax(x, __shfl_xor_sync(0xffffffffu, x, off));
+        y = tmax(y, __shfl_xor_sync(0xffffffffu, y, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = x;
+        red[1][threadIdx.x >> 5] = y;
+    }
+    const int any = __syncthreads_or(flag ? 1 : 0);
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < NT / 32; w++) {
+            x = tmax(x, red[0][w]);
+            y = tmax(y, red[1][w]);
+        }
+    }
+    return any;
+}
+
+
+}  // namespace gclaw

@@ -195,3 +195,66 @@ def make_claw(w: Workload, precision="fp64"):
         claw.tfinal = w.tfinal
         claw.num_output_times = w.num_output_times
     return claw
+
+
+BATCH_SEED = 20261205
+
+
+@dataclass
+class Ensemble:
+    """Many independent shallow-water problems on [0,1]^2 with wall BCs."""
+    shapes: list
+    deltas: list
+    params: list   # per problem (a, b, x0, y0)
+    dt0: np.ndarray
+    grav: float = 1.0
+    cfl_desired: float = 0.9
+    cfl_max: float = 1.0
+    nsteps: int = 200
+    seed: int = BATCH_SEED
+
+    @property
+    def cells(self):
+        return int(sum(a * b for a, b in self.shapes))
+
+    def q0(self, p):
+        """Initial state (3, mx, my) of problem p: h = 1 + a exp(-b |x - x0|^2)."""
+        mx, my = self.shapes[p]
+        a, b, x0, y0 = self.params[p]
+        X, Y = np.meshgrid(_centers(0.0, 1.0, mx), _centers(0.0, 1.0, my), indexing="ij")
+        q = np.zeros((3, mx, my), order="F")
+        q[0] = 1.0 + a * np.exp(-b * ((X - x0) ** 2 + (Y - y0) ** 2))
+        return q
+
+
+def batched_ensemble(nprob=4096, smin=32, smax=512, nsteps=200, seed=BATCH_SEED):
+    """4096 shallow-water problems, square grids with side log-uniform in
+    [smin, smax]; h = 1 + a exp(-b |x-x0|^2), a in U[0.05, 0.5], b in
+    U[20, 200], x0 uniform in the domain; hu = hv = 0; first dt of each
+    problem from its own initial wave speed at CFL 0.9."""
+    rng = np.random.default_rng(seed)
+    sides = np.rint(np.exp(rng.uniform(math.log(smin), math.log(smax), nprob))).astype(int)
+    a = rng.uniform(0.05, 0.5, nprob)
+    b = rng.uniform(20.0, 200.0, nprob)
+    x0 = rng.uniform(0.0, 1.0, (nprob, 2))
+    shapes = [(int(s), int(s)) for s in sides]
+    deltas = [(1.0 / s, 1.0 / s) for s in sides]
+    params = [(float(a[p]), float(b[p]), float(x0[p, 0]), float(x0[p, 1])) for p in range(nprob)]
+    dt0 = np.array([0.9 * (1.0 / s) / math.sqrt(1.0 * (1.0 + ap)) for s, ap in zip(sides, a)])
+    return Ensemble(shapes, deltas, params, dt0, nsteps=nsteps, seed=seed)
+
+
+def make_batch(e: Ensemble, precision=_lib.PREC_FP32_BULK, device=None):
+    """A BatchSolver loaded with ensemble e's initial states and controls."""
+    from .batch import BatchSolver
+
+    bs = BatchSolver(_lib.RP_SHALLOW_ROE_WITH_EFIX_2D, e.shapes, e.deltas, [BC.wall, BC.wall],
+                     [BC.wall, BC.wall], [tvd.MC] * 3, [e.grav], precision=precision,
+                     device=device)
+    host = bs.pinned_host_buffer()
+    for p in range(len(e.shapes)):
+        bs.pack(host, p, e.q0(p))
+    bs.upload(host)
+    bs.ctrl_init(e.dt0, cfl_max=e.cfl_max, cfl_desired=e.cfl_desired, max_accepted=e.nsteps,
+                 max_steps=10 * e.nsteps)
+    return bs

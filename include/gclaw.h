@@ -187,6 +187,44 @@ int gclaw_evolve_host(const gclaw_solver *s, const double *q_host, double *q_out
                       double cfl_desired, double dt_max, int max_steps, void *ws_dev,
                       size_t ws_bytes, int batch, gclaw_ctrl *ctrl_out, void *stream);
 
+/* ---- batches of independent problems ------------------------------------
+ * Many problems of uneven grid sizes that share one gclaw_solver (its rp,
+ * boundary conditions, limiters, order, transverse_waves, precision and
+ * problem_data; its mx, my, dx, dy are ignored) advance together: each
+ * launch is one attempted step of every unfinished problem, with per-problem
+ * dt, CFL, rejection and stop (PyClaw's evolve_to_time rules per problem).
+ * There is no reference counterpart in one call; PyClaw users loop over
+ * solvers.  States of all problems live in two caller-owned FP64 buffers,
+ * problem p at q_offset[p] (in doubles), each in the single-problem layout. */
+typedef struct gclaw_batch_problem {
+    int mx, my;          /* interior cells, >= 2 */
+    double dx, dy;       /* cell sizes */
+    long long q_offset;  /* offset of the problem's state in the buffers (doubles) */
+} gclaw_batch_problem;
+
+/* Device bytes of the tile table for nprob problems. */
+size_t gclaw_batch_table_bytes(int nprob);
+
+/* Fill the tile table (caller-owned device memory, 16-byte aligned) for the
+ * problems described in host memory; returns the total number of tiles in
+ * *total_tiles.  Synchronises the stream. */
+int gclaw_batch_prepare(const gclaw_solver *s, const gclaw_batch_problem *probs, int nprob,
+                        void *table_dev, size_t table_bytes, int *total_tiles, void *stream);
+
+/* Initialise nprob control blocks (an array of gclaw_ctrl in device memory);
+ * dt0_dev[p] is problem p's first dt (device array of nprob doubles). */
+int gclaw_batch_ctrl_init(gclaw_ctrl *ctrls_dev, int nprob, const double *dt0_dev, double t,
+                          double t_end, double cfl_max, double cfl_desired, double dt_max,
+                          int max_steps, int max_accepted, int dt_variable, void *stream);
+
+/* Enqueue nlaunch batched steps (no synchronisation; capturable in a CUDA
+ * graph).  Each launch is a persistent grid of resident CTAs striding over
+ * all tiles of all problems; problem p's accepted state is in q0 or q1 per
+ * ctrls_dev[p].parity. */
+int gclaw_batch_advance(const gclaw_solver *s, const void *table_dev, int nprob, int total_tiles,
+                        double *q0_dev, double *q1_dev, gclaw_ctrl *ctrls_dev, int nlaunch,
+                        void *stream);
+
 /* Allocation-free variant of gclaw_step2 (no counterpart in the reference,
  * whose Fortran step needs no device memory).  For callers that cannot
  * allocate device memory or hand over a workspace -- a Fortran/C host code

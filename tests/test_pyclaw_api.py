@@ -76,3 +76,22 @@ def test_workloads_shapes():
     e = workloads.euler_quadrants(16, 16)
     assert len(e.meta["states"]) == 4 and e.q0.shape == (4, 16, 16)
     assert np.all(e.q0[0] > 0)
+
+
+def test_batched_ensemble_shapes_and_sizes():
+    e = workloads.batched_ensemble()
+    sides = np.array([s[0] for s in e.shapes])
+    assert len(sides) == 4096 and sides.min() >= 32 and sides.max() <= 512
+    # log-uniform sides: mean cells per problem near (512^2 - 32^2) / (2 ln 16)
+    assert 40000 < e.cells / 4096 < 55000
+    q = e.q0(3)
+    assert q.shape == (3,) + e.shapes[3] and np.all(q[0] >= 1.0) and np.all(q[1:] == 0.0)
+    assert np.all(e.dt0 > 0)
+
+
+def test_batch_table_size():
+    from clawpack_gb300 import _lib
+
+    L = _lib.lib()
+    assert L.gclaw_batch_table_bytes(10) == 10 * 48 + 11 * 4
+    assert L.gclaw_batch_table_bytes(0) == 0
