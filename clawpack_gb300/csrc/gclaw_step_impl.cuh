@@ -469,6 +469,39 @@ static __device__ void finish_step(gclaw_ctrl *c, int ctrl_mode, double dt, doub
     }
 }
 
+// ---- tile load ---------------------------------------------------------------
+// The tile at (i0, j0) plus its 2-cell halo into QS (SoA planes, row stride
+// QW).  When the whole window lies inside the input array (every tile but
+// the boundary ones) it is read row by row with coalesced loads; otherwise
+// each value goes through the boundary conditions (load_q).
+template <class RP, typename T, int TX, int TY, int NT>
+__device__ __forceinline__ void load_tile(const StepArgs &a, const double *__restrict__ qin, int i0,
+                                          int j0, T *QS) {
+    using TL = Tile<RP, TX, TY>;
+    constexpr int M = RP::M;
+    const int off = a.ghosted ? 2 : 0, nx = a.mx + 2 * off, ny = a.my + 2 * off;
+    const bool inside = i0 - 2 + off >= 0 && i0 + TX + 2 + off <= nx && j0 - 2 + off >= 0 &&
+                        j0 + TY + 2 + off <= ny;
+    if (inside) {
+        constexpr int RW = (TX + 4) * M;  // doubles per tile row
+        const double *__restrict__ base =
+            qin + (size_t)M * ((size_t)(i0 - 2 + off) + (size_t)nx * (size_t)(j0 - 2 + off));
+        const size_t rs = (size_t)M * (size_t)nx;
+        for (int idx = threadIdx.x; idx < RW * TL::QH; idx += NT) {
+            const int r = idx / RW, c = idx - r * RW;
+            const int cell = c / M, k = c - cell * M;
+            QS[k * TL::QN + r * TL::QW + cell] = from_double<T>(__ldg(base + r * rs + c));
+        }
+    } else {
+        for (int idx = threadIdx.x; idx < (TX + 4) * TL::QH * M; idx += NT) {
+            const int k = idx % M, cell = idx / M;
+            const int cx = cell % (TX + 4), cy = cell / (TX + 4);
+            QS[k * TL::QN + cy * TL::QW + cx] =
+                from_double<T>(load_q<M>(a, qin, k, i0 - 2 + cx, j0 - 2 + cy));
+        }
+    }
+}
+
 // ---- one tile, both sweeps --------------------------------------------------
 // Runs the whole step for the tile at (i0, j0): load with boundary
 // conditions, both sweeps, and the write of the new state.  Returns the
@@ -492,31 +525,7 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, const typename RPT<
     T *CA = EB;
     const T tdtdx = (T)dtdx, tdtdy = (T)dtdy;
 
-    // L: tile + halo.  When the whole window lies inside the input array
-    // (every tile but the boundary ones) it is read row by row with
-    // coalesced loads; otherwise each value goes through the boundary
-    // conditions (load_q).
-    const int off = a.ghosted ? 2 : 0, nx = a.mx + 2 * off, ny = a.my + 2 * off;
-    const bool inside = i0 - 2 + off >= 0 && i0 + TX + 2 + off <= nx && j0 - 2 + off >= 0 &&
-                        j0 + TY + 2 + off <= ny;
-    if (inside) {
-        constexpr int RW = (TX + 4) * M;  // doubles per tile row
-        const double *__restrict__ base =
-            qin + (size_t)M * ((size_t)(i0 - 2 + off) + (size_t)nx * (size_t)(j0 - 2 + off));
-        const size_t rs = (size_t)M * (size_t)nx;
-        for (int idx = threadIdx.x; idx < RW * TL::QH; idx += NT) {
-            const int r = idx / RW, c = idx - r * RW;
-            const int cell = c / M, k = c - cell * M;
-            QS[k * TL::QN + r * TL::QW + cell] = from_double<T>(__ldg(base + r * rs + c));
-        }
-    } else {
-        for (int idx = threadIdx.x; idx < (TX + 4) * TL::QH * M; idx += NT) {
-            const int k = idx % M, cell = idx / M;
-            const int cx = cell % (TX + 4), cy = cell / (TX + 4);
-            QS[k * TL::QN + cy * TL::QW + cx] =
-                from_double<T>(load_q<M>(a, qin, k, i0 - 2 + cx, j0 - 2 + cy));
-        }
-    }
+    load_tile<RP, T, TX, TY, NT>(a, qin, i0, j0, QS);
     __syncthreads();
 
     A acc[NC][M];

@@ -258,3 +258,66 @@ def make_batch(e: Ensemble, precision=_lib.PREC_FP32_BULK, device=None):
     bs.ctrl_init(e.dt0, cfl_max=e.cfl_max, cfl_desired=e.cfl_desired, max_accepted=e.nsteps,
                  max_steps=10 * e.nsteps)
     return bs
+
+
+ADJOINT_SEED = 20261206
+
+
+@dataclass
+class AdjointProblem:
+    """Least-squares fit of gauge series: shallow water on [0,1]^2, wall BCs,
+    MC limiter, transverse_waves 2; h0 = 1 + sum of 16 seeded Gaussians of
+    amplitude <= 0.2; loss = sum over steps and 64 gauge cells of
+    (h - target)^2, targets from a run of a second seeded initial surface."""
+    mx: int
+    my: int
+    nsteps: int
+    checkpoint_every: int
+    h0: np.ndarray
+    h_true: np.ndarray
+    gauges: np.ndarray  # (64, 2) cell indices (i, j)
+    grav: float = 1.0
+    cfl_desired: float = 0.9
+    limiter: int = tvd.MC
+
+    @property
+    def dx(self):
+        return 1.0 / self.mx
+
+    def q0(self, h=None):
+        q = np.zeros((3, self.mx, self.my), order="F")
+        q[0] = self.h0 if h is None else h
+        return q
+
+    def solver_struct(self, precision=_lib.PREC_FP64):
+        from .device import make_solver_struct
+
+        return make_solver_struct(_lib.RP_SHALLOW_ROE_WITH_EFIX_2D, self.mx, self.my,
+                                  1.0 / self.mx, 1.0 / self.my, [BC.wall, BC.wall],
+                                  [BC.wall, BC.wall], [self.limiter] * 3, 2, 2, precision,
+                                  [self.grav])
+
+    @property
+    def dt0(self):
+        return self.cfl_desired * self.dx / math.sqrt(self.grav * float(self.h0.max()))
+
+
+def _bumps(rng, mx, my, n=16, amp=0.2):
+    X, Y = np.meshgrid(_centers(0.0, 1.0, mx), _centers(0.0, 1.0, my), indexing="ij")
+    h = np.ones((mx, my))
+    for _ in range(n):
+        a = rng.uniform(0.0, amp)
+        b = rng.uniform(50.0, 300.0)
+        x0, y0 = rng.uniform(0.1, 0.9, 2)
+        h += a * np.exp(-b * ((X - x0) ** 2 + (Y - y0) ** 2))
+    return h
+
+
+def adjoint_problem(mx=1024, my=None, nsteps=500, checkpoint_every=23, seed=ADJOINT_SEED,
+                    limiter=tvd.MC):
+    my = my or mx
+    rng = np.random.default_rng(seed)
+    h0 = _bumps(rng, mx, my)
+    h_true = _bumps(rng, mx, my)
+    gauges = np.stack([rng.integers(0, mx, 64), rng.integers(0, my, 64)], axis=1)
+    return AdjointProblem(mx, my, nsteps, checkpoint_every, h0, h_true, gauges, limiter=limiter)

@@ -225,6 +225,16 @@ int gclaw_batch_advance(const gclaw_solver *s, const void *table_dev, int nprob,
                         double *q0_dev, double *q1_dev, gclaw_ctrl *ctrls_dev, int nlaunch,
                         void *stream);
 
+/* Adjoint (reverse mode) of one step at fixed dt: lam_old = J^T lam_new with
+ * J = d step(q) / d q at q = q_dev, for gradients through time stepping
+ * (the reference has no adjoint).  Supported: GCLAW_RP_ACOUSTICS_2D and
+ * GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D, FP64 or FP32-bulk arithmetic, lam in
+ * FP64 with the layout of q.  The limiter, entropy-fix and transverse
+ * min/max branches are those the forward step takes on q_dev.  lam_old_dev
+ * must not alias lam_new_dev; it is overwritten.  No synchronisation. */
+int gclaw_adjoint_step(const gclaw_solver *s, const double *q_dev, const double *lam_new_dev,
+                       double *lam_old_dev, double dt, void *stream);
+
 /* Allocation-free variant of gclaw_step2 (no counterpart in the reference,
  * whose Fortran step needs no device memory).  For callers that cannot
  * allocate device memory or hand over a workspace -- a Fortran/C host code
