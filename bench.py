@@ -63,6 +63,7 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--batched-steps", type=int, default=200)
+    p.add_argument("--no-adjoint", action="store_true")
     return p.parse_args()
 
 
@@ -308,6 +309,56 @@ def bench_batched(args, torch, world, device):
             "rel_l1_vs_fp64_max_over_128_problems": max(errs)}
 
 
+def bench_adjoint(torch, world, device):
+    """Gradient of the gauge least-squares loss with respect to the initial
+    surface: 1024^2 shallow water, 500 steps, checkpoints every 23 steps,
+    64 gauges; forward + checkpointed backward through the hand-written
+    adjoint kernel, FP64 and FP32-bulk."""
+    from clawpack_gb300 import _lib, adjoint, workloads
+
+    p = workloads.adjoint_problem()
+    s64 = p.solver_struct(_lib.PREC_FP64)
+    dts = adjoint.record_dts(torch.from_numpy(p.q0()).to(device), s64, p.nsteps, p.dt0)
+    gauges = torch.as_tensor(p.gauges, device=device)
+    target = adjoint.gauge_series(torch.from_numpy(p.q0(p.h_true)).to(device), s64, dts, gauges)
+    warm = workloads.adjoint_problem(64, nsteps=8, checkpoint_every=3)
+    res, grads = {}, {}
+    for name, prec in (("fp64", _lib.PREC_FP64), ("fp32_bulk", _lib.PREC_FP32_BULK)):
+        for prob, d, tg in ((warm, dts[:8], None), (p, dts, target)):
+            h0 = torch.from_numpy(prob.h0).to(device).requires_grad_(True)
+            q = torch.stack([h0, torch.zeros_like(h0), torch.zeros_like(h0)])
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            torch.cuda.synchronize()
+            barrier(world)
+            ev[0].record()
+            series = adjoint.evolve_gauges(q, prob.solver_struct(prec), d,
+                                           torch.as_tensor(prob.gauges, device=device),
+                                           prob.checkpoint_every)
+            ev[1].record()
+            loss = ((series - (series.detach() * 0 if tg is None else tg)) ** 2).sum()
+            loss.backward()
+            ev[2].record()
+            torch.cuda.synchronize()
+        fwd = max_over_ranks(ev[0].elapsed_time(ev[1]) * 1e-3, world, device)
+        bwd = max_over_ranks(ev[1].elapsed_time(ev[2]) * 1e-3, world, device)
+        grads[name] = h0.grad.double().cpu().numpy()
+        cells = p.mx * p.my
+        n = len(dts)
+        res[name] = {"forward_s": round(fwd, 4), "backward_s": round(bwd, 4),
+                     "gradient_s": round(fwd + bwd, 4),
+                     "forward_gcell_updates_per_s": round(world * cells * n / fwd * 1e-9, 4),
+                     "backward_gcell_updates_per_s": round(world * cells * n / bwd * 1e-9, 4),
+                     "loss": float(loss.detach())}
+    a, b = grads["fp64"], grads["fp32_bulk"]
+    nseg = -(-len(dts) // p.checkpoint_every)
+    return {"workload": f"shallow water {p.mx}x{p.my}, {len(dts)} steps, 64 gauges, "
+                        f"checkpoints every {p.checkpoint_every} steps, MC, wall BCs",
+            "unit": "s per gradient", **res,
+            "fp32_vs_fp64_grad_rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(a)),
+            "launches_per_gradient": 2 * len(dts) + (len(dts) - nseg),
+            "launches": 2 * (2 * len(dts) + (len(dts) - nseg))}
+
+
 def cpu_baseline(w, target_s=15.0):
     """The CPU oracle on the host cores (OpenMP, all threads) over a bounded
     number of full-grid steps."""
@@ -325,7 +376,7 @@ def cpu_baseline(w, target_s=15.0):
     t0 = time.perf_counter()
     q, cfl, _ = one(q, dt)
     first = time.perf_counter() - t0
-    n = int(max(1, min(20, target_s / max(first, 1e-3))))
+    n = int(max(1, min(1000, target_s / max(first, 1e-3))))
     t0 = time.perf_counter()
     for _ in range(n):
         dt = dt * w.cfl_desired / cfl
@@ -411,6 +462,9 @@ def run_ours(args):
     if not args.no_batched:
         out["batched"] = bench_batched(args, torch, world, device)
         out["gpu_launches"] += out["batched"]["launches"]
+    if not args.no_adjoint:
+        out["adjoint"] = bench_adjoint(torch, world, device)
+        out["gpu_launches"] += out["adjoint"]["launches"]
     # end to end through the C ABI with host buffers, every step
     e2e_s, e2e_acc, qb = e2e_host_steps(w, args.e2e_steps, torch, device)
     e2e_s = max_over_ranks(e2e_s, world, device)

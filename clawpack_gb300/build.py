@@ -5,9 +5,11 @@
 Produces, next to this file:
   libgclaw.so         the product library (nvcc default contraction of
                       multiply-adds into FMA)
-  libgclaw_strict.so  the same sources with -fmad=false: every FP64 multiply
-                      and add rounded separately, for bit-for-bit comparison
-                      with the CPU oracle in the parity tests
+  libgclaw_strict.so  the same sources with -fmad=false and GCLAW_STRICT:
+                      every FP64 multiply and add rounded separately and every
+                      quotient and square root taken as the reference writes
+                      it, for bit-for-bit comparison with the CPU oracle in
+                      the parity tests
 Every (library, source) pair compiles to an object in parallel under
 _build/, then each library is linked.
 """
@@ -52,7 +54,7 @@ def _compile_cmd(src, obj, extra):
 def targets():
     return [
         (os.path.join(HERE, "libgclaw.so"), []),
-        (os.path.join(HERE, "libgclaw_strict.so"), ["-fmad=false"]),
+        (os.path.join(HERE, "libgclaw_strict.so"), ["-fmad=false", "-DGCLAW_STRICT"]),
     ]
 
 

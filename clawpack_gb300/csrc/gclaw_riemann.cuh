@@ -43,6 +43,22 @@ __device__ __forceinline__ float tmin<float>(float a, float b) { return fminf(a,
 template <>
 __device__ __forceinline__ float tmax<float>(float a, float b) { return fmaxf(a, b); }
 
+// True when fl(m / h - sqrt(g h)) > 0 cannot hold, decided without the
+// division and the square root: h > 0 and either m <= 0 (the quotient is
+// not positive) or m^2 < 0.81 g h^3 (|m / h| < 0.9 sqrt(g h) exactly, a
+// margin no rounding of either side can close).  A normal-range bound on the
+// right side keeps underflow and flush-to-zero out of the test; NaN and
+// infinite inputs fall through to the exact evaluation.  Used to skip the
+// intermediate-state speeds of the entropy fix when the transonic test is
+// certain to fail (every subsonic edge), with unchanged branch decisions.
+template <typename T>
+__device__ __forceinline__ bool no_right_sonic_point(T h, T m, T g) {
+    if (!(h > (T)0)) return false;
+    if (m <= (T)0) return true;
+    const T rhs = (T)0.81 * g * h * h * h;
+    return rhs >= (sizeof(T) == 8 ? (T)1e-290 : (T)1e-30) && m * m < rhs;
+}
+
 // ---------------------------------------------------------------------------
 // Constant-coefficient acoustics: q = (p, u, v); speeds -c, +c.
 // ---------------------------------------------------------------------------
@@ -55,6 +71,10 @@ struct RpAcoustics {
     static Params make(const double *pd) { return Params{(T)pd[2], (T)pd[3]}; }
 
     __device__ __forceinline__ static void cell_aux(const Params &P, const T *q, T *aux) {}
+
+    // components of wave p that can be nonzero in direction IXY
+    template <int IXY>
+    __host__ __device__ static constexpr bool wnz(int p, int k) { return k != 3 - IXY; }
 
     template <int IXY>
     __device__ __forceinline__ static bool rpn2(const Params &P, const T *ql, const T *qr,
@@ -114,18 +134,35 @@ struct RpShallow {
     struct Params {
         T g;
         double gd;
+        T sg;  // sqrt(g)
     };
-    static Params make(const double *pd) { return Params{(T)pd[0], pd[0]}; }
+    static Params make(const double *pd) { return Params{(T)pd[0], pd[0], (T)sqrt(pd[0])}; }
 
-    // aux = (sqrt h, hu / sqrt h, hv / sqrt h, hu / h, hv / h, sqrt(g h))
+    // the shear wave carries only the transverse momentum
+    template <int IXY>
+    __host__ __device__ static constexpr bool wnz(int p, int k) { return p != 1 || k == 3 - IXY; }
+
+    // aux = (sqrt h, hu / sqrt h, hv / sqrt h, hu / h, hv / h, sqrt(g h)).
+    // GCLAW_STRICT evaluates each as written; otherwise one square root and
+    // one reciprocal per cell (hu / sqrt h = (hu / h) sqrt h, sqrt(g h) =
+    // sqrt(g) sqrt h), within two roundings of the quotients.
     __device__ __forceinline__ static void cell_aux(const Params &P, const T *q, T *aux) {
         const T hs = sqrt(q[0]);
         aux[0] = hs;
+#ifdef GCLAW_STRICT
         aux[1] = q[1] / hs;
         aux[2] = q[2] / hs;
         aux[3] = q[1] / q[0];
         aux[4] = q[2] / q[0];
         aux[5] = sqrt(P.g * q[0]);
+#else
+        const T rh = (T)1 / q[0];
+        aux[3] = q[1] * rh;
+        aux[4] = q[2] * rh;
+        aux[1] = aux[3] * hs;
+        aux[2] = aux[4] * hs;
+        aux[5] = P.sg * hs;
+#endif
     }
 
     // Roe state R = (ubar, vbar, cbar, 0.5 / cbar).  In FP32-bulk mode,
@@ -144,10 +181,21 @@ struct RpShallow {
             c = (T)sqrt(P.gd * (((double)hl + (double)hr) * 0.5));
         } else {
             const T hsq2 = al[0] + ar[0];
+            const T hbar = (hl + hr) * (T)0.5;
+#ifdef GCLAW_STRICT
             u = (al[mu] + ar[mu]) / hsq2;
             v = (al[mv] + ar[mv]) / hsq2;
-            const T hbar = (hl + hr) * (T)0.5;
             c = sqrt(P.g * hbar);
+#else
+            // one reciprocal for both averages; c and 0.5 / c from one rsqrt
+            const T ri = (T)1 / hsq2;
+            u = (al[mu] + ar[mu]) * ri;
+            v = (al[mv] + ar[mv]) * ri;
+            const T gh = P.g * hbar;
+            const T rs = rsqrt(gh);
+            R[0] = u; R[1] = v; R[2] = gh * rs; R[3] = (T)0.5 * rs;
+            return;
+#endif
         }
         R[0] = u; R[1] = v; R[2] = c; R[3] = (T)0.5 / c;
     }
@@ -181,9 +229,13 @@ struct RpShallow {
         } else {
             T h1 = hl + w1[0];
             T hu1 = ql[mu] + w1[mu];
-            T s1 = hu1 / h1 - sqrt(g * h1);
-            T sfract;
-            if (s0 < (T)0 && s1 > (T)0)
+            T s1 = (T)0, sfract;
+            bool sonic1 = false;  // s0 < 0 < s1: transonic 1-rarefaction
+            if (s0 < (T)0 && !no_right_sonic_point(h1, hu1, g)) {
+                s1 = hu1 / h1 - sqrt(g * h1);
+                sonic1 = s1 > (T)0;
+            }
+            if (sonic1)
                 sfract = s0 * (s1 - s[0]) / (s1 - s0);
             else if (s[0] < (T)0)
                 sfract = s[0];
@@ -197,9 +249,14 @@ struct RpShallow {
                 const T s03 = ar[2 + mu] + ar[5];  // u + c in the right cell
                 T h3 = hr - w3[0];
                 T hu3 = qr[mu] - w3[mu];
-                T s3 = hu3 / h3 + sqrt(g * h3);
+                T s3 = (T)0;
+                bool sonic3 = false;  // s3 < 0 < s03: transonic 3-rarefaction
+                if (s03 > (T)0 && !no_right_sonic_point(h3, -hu3, g)) {
+                    s3 = hu3 / h3 + sqrt(g * h3);
+                    sonic3 = s3 < (T)0;
+                }
                 bool add = true;
-                if (s3 < (T)0 && s03 > (T)0)
+                if (sonic3)
                     sfract = s3 * (s03 - s[2]) / (s03 - s3);
                 else if (s[2] < (T)0)
                     sfract = s[2];
@@ -254,6 +311,12 @@ struct RpEuler {
     };
     static Params make(const double *pd) {
         return Params{(T)pd[0], (T)(pd[0] - 1.0), pd[1] != 0.0 ? 1 : 0};
+    }
+
+    // the shear wave (third) has no density and no normal momentum
+    template <int IXY>
+    __host__ __device__ static constexpr bool wnz(int p, int k) {
+        return p != 2 || (k != 0 && k != IXY);
     }
 
     __device__ __forceinline__ static T pressure(T gamma1, const T *q) {

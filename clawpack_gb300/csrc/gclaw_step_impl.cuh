@@ -261,7 +261,8 @@ __device__ __forceinline__ void phase_rpn2(const typename RP::Params &P, const T
         T W[MW * M], s[MW], am[M], ap[M], R[NR > 0 ? NR : 1];
         bad |= RP::template rpn2<IXY>(P, ql, qr, al, ar, W, s, am, ap, R);
 #pragma unroll
-        for (int f = 0; f < MW * M; f++) EA[(TL::FW + f) * TL::NE1 + it] = W[f];
+        for (int f = 0; f < MW * M; f++)
+            if (RP::template wnz<IXY>(f / M, f % M)) EA[(TL::FW + f) * TL::NE1 + it] = W[f];
 #pragma unroll
         for (int p = 0; p < MW; p++) EA[(TL::FS + p) * TL::NE1 + it] = s[p];
 #pragma unroll
@@ -295,8 +296,11 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
         SI::split2(it, e2, sl);
         const int ie = SI::item1(e2 + 1, sl);
         T W[MW * M], s[MW], am[M], ap[M], cq[M];
+        // components that are zero by the solver's eigenstructure are neither
+        // stored nor loaded; the sums below then skip exact +0 terms
 #pragma unroll
-        for (int f = 0; f < MW * M; f++) W[f] = EA[(TL::FW + f) * TL::NE1 + ie];
+        for (int f = 0; f < MW * M; f++)
+            W[f] = RP::template wnz<IXY>(f / M, f % M) ? EA[(TL::FW + f) * TL::NE1 + ie] : (T)0;
 #pragma unroll
         for (int p = 0; p < MW; p++) s[p] = EA[(TL::FS + p) * TL::NE1 + ie];
 #pragma unroll
@@ -312,17 +316,20 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
                 if (lim == 0) continue;
                 T wn2 = (T)0;
 #pragma unroll
-                for (int k = 0; k < M; k++) wn2 = wn2 + W[p * M + k] * W[p * M + k];
+                for (int k = 0; k < M; k++)
+                    if (RP::template wnz<IXY>(p, k)) wn2 = wn2 + W[p * M + k] * W[p * M + k];
                 if (wn2 == (T)0) continue;
                 T dot = (T)0;
                 if (s[p] > (T)0) {
 #pragma unroll
                     for (int k = 0; k < M; k++)
-                        dot = dot + EA[(TL::FW + p * M + k) * TL::NE1 + ie - STEP] * W[p * M + k];
+                        if (RP::template wnz<IXY>(p, k))
+                            dot = dot + EA[(TL::FW + p * M + k) * TL::NE1 + ie - STEP] * W[p * M + k];
                 } else {
 #pragma unroll
                     for (int k = 0; k < M; k++)
-                        dot = dot + W[p * M + k] * EA[(TL::FW + p * M + k) * TL::NE1 + ie + STEP];
+                        if (RP::template wnz<IXY>(p, k))
+                            dot = dot + W[p * M + k] * EA[(TL::FW + p * M + k) * TL::NE1 + ie + STEP];
                 }
                 const T phi = philim<T>(lim, dot / wn2);
 #pragma unroll
@@ -334,6 +341,7 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
                 T c = (T)0;
 #pragma unroll
                 for (int p = 0; p < MW; p++) {
+                    if (!RP::template wnz<IXY>(p, k)) continue;
                     const T sa = fabs(s[p]);
                     c = c + sa * ((T)1 - sa * dtave) * W[p * M + k];
                 }
