@@ -5,7 +5,10 @@
 
 Advances the chosen problem by --warmup then --steps device-controlled steps
 (one step kernel each) and prints one JSON line with the mean step time from
-CUDA events.  Used for profiling captures and quick size sweeps.
+CUDA events.  With --adjoint, the --warmup + --steps launches time adjoint
+steps (gclaw_adjoint_step) instead, about the state after one forward step,
+with a seeded random adjoint field.  Used for profiling captures and quick
+size sweeps.
 """
 from __future__ import annotations
 
@@ -37,12 +40,16 @@ def main(argv=None):
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    p.add_argument("--adjoint", action="store_true")
     a = p.parse_args(argv)
     w = make_workload(a.workload, a.mx, a.my or a.mx)
-    dev = DeviceProblem(w.solver_struct(0 if a.precision == "fp64" else 1))
+    s = w.solver_struct(0 if a.precision == "fp64" else 1)
+    dev = DeviceProblem(s)
     dev.upload(w.q0)
     dev.ctrl_init(0.0, w.dt_initial, math.inf, cfl_max=w.cfl_max, cfl_desired=w.cfl_desired,
                   max_steps=10 ** 9)
+    if a.adjoint:
+        return run_adjoint(a, w, s, dev)
     dev.advance(a.warmup)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -57,6 +64,33 @@ def main(argv=None):
                       "gcell_updates_per_s": cells / (ms * 1e-3) * 1e-9 if ms > 0 else None,
                       "accepted": c.numsteps, "status": c.status, "cfl": c.cfl}))
     return 0 if c.status == 0 else 1
+
+
+def run_adjoint(a, w, s, dev):
+    from .adjoint import _Stepper
+
+    dev.advance(1)
+    c = dev.read_ctrl()
+    q = dev.q[c.parity]
+    st = _Stepper(s, q.device)
+    gen = torch.Generator(device=q.device).manual_seed(5)
+    lam = torch.randn(q.shape, dtype=q.dtype, device=q.device, generator=gen)
+    for _ in range(a.warmup):
+        lam = st.adjoint(q, lam, c.dt)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.steps):
+        lam = st.adjoint(q, lam, c.dt)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(a.steps, 1)
+    finite = bool(torch.isfinite(lam).all())
+    print(json.dumps({"workload": w.name, "mx": w.mx, "my": w.my, "precision": a.precision,
+                      "adjoint_steps": a.steps, "ms_per_step": ms,
+                      "gcell_updates_per_s": w.mx * w.my / (ms * 1e-3) * 1e-9 if ms > 0 else None,
+                      "finite": finite}))
+    return 0 if finite else 1
 
 
 if __name__ == "__main__":
