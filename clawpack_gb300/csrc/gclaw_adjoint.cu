@@ -38,13 +38,17 @@ struct AdjTile {
     static constexpr int NA = RP::NA > 0 ? RP::NA : 1;
     static constexpr int NR = RP::NR > 0 ? RP::NR : 1;
     static constexpr int QN = TL::QN, NE1 = TL::NE1;
+    // forward edge records with every wave component: W[MW*M], s[MW],
+    // amdq[M], apdq[M], Roe state[NR]
+    static constexpr int FW = 0, FS = MW * M, FAM = FS + MW, FAP = FAM + M, FR = FAP + M;
+    static constexpr int EAW = FR + RP::NR;
     // adjoint slots per edge: own W, s, amdq, apdq, Roe state, and W from
     // the left / right neighbour edge's limiter
     static constexpr int GW = 0, GS = MW * M, GAM = GS + MW, GAP = GAM + M, GR = GAP + M;
     static constexpr int GWL = GR + NR, GWR = GWL + MW * M, GBW = GWR + MW * M;
     template <typename T>
     static constexpr size_t smem_bytes() {
-        return sizeof(T) * ((size_t)M * QN + (size_t)NA * QN + (size_t)TL::EAW * NE1 +
+        return sizeof(T) * ((size_t)M * QN + (size_t)NA * QN + (size_t)EAW * NE1 +
                             (size_t)GBW * NE1 + (size_t)M * TX * TY + (size_t)M * QN);
     }
 };
@@ -88,16 +92,16 @@ __device__ __forceinline__ void adj_sweep(const StepArgs &a, const typename RP::
         T W[MW * M], s[MW], am[M], ap[M], R[ANR];
         RP::template rpn2<IXY>(P, ql, qr, al, ar, W, s, am, ap, R);
 #pragma unroll
-        for (int f = 0; f < MW * M; f++) EA[(TL::FW + f) * TL::NE1 + it] = W[f];
+        for (int f = 0; f < MW * M; f++) EA[(AT::FW + f) * TL::NE1 + it] = W[f];
 #pragma unroll
-        for (int p = 0; p < MW; p++) EA[(TL::FS + p) * TL::NE1 + it] = s[p];
+        for (int p = 0; p < MW; p++) EA[(AT::FS + p) * TL::NE1 + it] = s[p];
 #pragma unroll
         for (int k = 0; k < M; k++) {
-            EA[(TL::FAM + k) * TL::NE1 + it] = am[k];
-            EA[(TL::FAP + k) * TL::NE1 + it] = ap[k];
+            EA[(AT::FAM + k) * TL::NE1 + it] = am[k];
+            EA[(AT::FAP + k) * TL::NE1 + it] = ap[k];
         }
 #pragma unroll
-        for (int r = 0; r < NR; r++) EA[(TL::FR + r) * TL::NE1 + it] = R[r];
+        for (int r = 0; r < NR; r++) EA[(AT::FR + r) * TL::NE1 + it] = R[r];
 #pragma unroll 1
         for (int f = 0; f < AT::GBW; f++) GB[f * AT::NE1 + it] = (T)0;
     }
@@ -137,17 +141,17 @@ __device__ __forceinline__ void adj_sweep(const StepArgs &a, const typename RP::
         // forward recompute of the limited waves and folded fluctuations
         T W[MW * M], s[MW], am[M], ap[M], R[ANR], cq[M];
 #pragma unroll
-        for (int f = 0; f < MW * M; f++) W[f] = EA[(TL::FW + f) * TL::NE1 + ie];
+        for (int f = 0; f < MW * M; f++) W[f] = EA[(AT::FW + f) * TL::NE1 + ie];
 #pragma unroll
-        for (int p = 0; p < MW; p++) s[p] = EA[(TL::FS + p) * TL::NE1 + ie];
+        for (int p = 0; p < MW; p++) s[p] = EA[(AT::FS + p) * TL::NE1 + ie];
 #pragma unroll
         for (int k = 0; k < M; k++) {
-            am[k] = EA[(TL::FAM + k) * TL::NE1 + ie];
-            ap[k] = EA[(TL::FAP + k) * TL::NE1 + ie];
+            am[k] = EA[(AT::FAM + k) * TL::NE1 + ie];
+            ap[k] = EA[(AT::FAP + k) * TL::NE1 + ie];
             cq[k] = (T)0;
         }
 #pragma unroll
-        for (int r = 0; r < NR; r++) R[r] = EA[(TL::FR + r) * TL::NE1 + ie];
+        for (int r = 0; r < NR; r++) R[r] = EA[(AT::FR + r) * TL::NE1 + ie];
         T phi[MW], theta[MW], wn2v[MW];
         int upd[MW];  // -1: upwind neighbour is the previous edge, +1: next, 0: not limited
         const T dtave = (T)0.5 * (dtdn + dtdn);
@@ -168,7 +172,7 @@ __device__ __forceinline__ void adj_sweep(const StepArgs &a, const typename RP::
                 T dot = (T)0;
 #pragma unroll
                 for (int k = 0; k < M; k++)
-                    dot = dot + EA[(TL::FW + p * M + k) * TL::NE1 + nb] * W[p * M + k];
+                    dot = dot + EA[(AT::FW + p * M + k) * TL::NE1 + nb] * W[p * M + k];
                 theta[p] = dot / wn2;
                 phi[p] = philim<T>(lim, theta[p]);
             }
@@ -248,7 +252,7 @@ __device__ __forceinline__ void adj_sweep(const StepArgs &a, const typename RP::
                 const int slot = upd[p] < 0 ? AT::GWR : AT::GWL;
 #pragma unroll
                 for (int k = 0; k < M; k++) {
-                    const T wn = EA[(TL::FW + p * M + k) * TL::NE1 + nb];
+                    const T wn = EA[(AT::FW + p * M + k) * TL::NE1 + nb];
                     Wb[p * M + k] += dotb * wn + (T)2 * wn2b * W[p * M + k];
                     GB[(slot + p * M + k) * AT::NE1 + nb] = dotb * W[p * M + k];
                 }
@@ -348,7 +352,7 @@ __global__ void __launch_bounds__(NT, 1)
     T *QS = reinterpret_cast<T *>(smem_raw);
     T *CA = QS + M * TL::QN;
     T *EA = CA + AT::NA * TL::QN;
-    T *GB = EA + TL::EAW * TL::NE1;
+    T *GB = EA + AT::EAW * TL::NE1;
     T *LT = GB + AT::GBW * TL::NE1;
     T *LA = LT + M * TX * TY;
     const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;

@@ -293,7 +293,22 @@ struct RpShallow {
         sb[1] = vbar;
         wb[6] = a3; wb[6 + mu] = a3 * ubar; wb[6 + mv] = a3 * (vbar + cbar);
         sb[2] = vbar + cbar;
-        split_sum<T, 3, 3>(sb, wb, bm, bp);
+        if (sb[0] <= (T)0 && sb[2] >= (T)0) {
+            // Subsonic across the edge (the usual case): the first wave
+            // goes only down, the third only up, and the shear wave has
+            // one component, so the sums of split_sum reduce to these
+            // terms; the dropped terms are exact zeros.
+            const T m1 = tmin(sb[1], (T)0), p1 = tmax(sb[1], (T)0);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                bm[k] = sb[0] * wb[k];
+                bp[k] = sb[2] * wb[6 + k];
+            }
+            bm[mu] = bm[mu] + m1 * a2;
+            bp[mu] = p1 * a2 + bp[mu];
+        } else {
+            split_sum<T, 3, 3>(sb, wb, bm, bp);
+        }
     }
 };
 

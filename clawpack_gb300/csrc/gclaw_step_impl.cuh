@@ -184,6 +184,28 @@ static inline void tile_shape(int rp, int precision, int *tx, int *ty) {
     }
 }
 
+// Wave components a solver can make nonzero (the same count in both
+// directions), and the compact shared-memory plane of component k of wave p
+// in direction IXY: components that are zero by the eigenstructure get no
+// plane.
+template <class RP>
+__host__ __device__ constexpr int wave_planes() {
+    int n = 0;
+    for (int p = 0; p < RP::MW; p++)
+        for (int k = 0; k < RP::M; k++) n += RP::template wnz<1>(p, k) ? 1 : 0;
+    return n;
+}
+template <class RP, int IXY>
+__host__ __device__ constexpr int wave_plane(int p, int k) {
+    int n = 0;
+    for (int pp = 0; pp < RP::MW; pp++)
+        for (int kk = 0; kk < RP::M; kk++) {
+            if (pp == p && kk == k) return n;
+            n += RP::template wnz<IXY>(pp, kk) ? 1 : 0;
+        }
+    return n;
+}
+
 template <class RP, int TX, int TY>
 struct Tile {
     static constexpr int M = RP::M, MW = RP::MW, NR = RP::NR, NA = RP::NA;
@@ -194,17 +216,30 @@ struct Tile {
     static constexpr int NE1 = NE1X > NE1Y ? NE1X : NE1Y;
     static constexpr int NE2X = (TX + 1) * (TY + 2), NE2Y = (TX + 2) * (TY + 1);
     static constexpr int NE2 = NE2X > NE2Y ? NE2X : NE2Y;
-    // edge area fields: W[MW*M], s[MW], amdq[M], apdq[M], Roe state[NR]
-    static constexpr int FW = 0, FS = MW * M, FAM = FS + MW, FAP = FAM + M, FR = FAP + M;
+    // edge area fields: nonzero wave components, s[MW], amdq[M], apdq[M],
+    // Roe state[NR]
+    static constexpr int NWP = wave_planes<RP>();
+    static constexpr int FW = 0, FS = NWP, FAM = FS + MW, FAP = FAM + M, FR = FAP + M;
     static constexpr int EAW = FR + NR;
     // second-phase fields: fadd, B-A-, B+A-, B-A+, B+A+ (each M)
     static constexpr int GFA = 0, GMM = M, GPM = 2 * M, GMP = 3 * M, GPP = 4 * M, EBW = 5 * M;
-    // the per-cell aux values of a sweep live in the second-phase area,
-    // which is free while the sweep's Riemann problems are solved
-    static_assert(NA * QN <= EBW * NE2, "cell aux area does not fit");
+    // The per-cell aux values get their own area, computed once per tile for
+    // both sweeps, when that still fits the occupancy the kernel is built
+    // for (one CTA per SM in FP64, two in FP32); otherwise each sweep
+    // computes them into the second-phase area, which is free while the
+    // sweep's Riemann problems are solved.
     template <typename T>
-    static constexpr size_t smem_bytes() {
+    __host__ __device__ static constexpr size_t base_bytes() {
         return sizeof(T) * ((size_t)M * QN + (size_t)EAW * NE1 + (size_t)EBW * NE2);
+    }
+    template <typename T>
+    __host__ __device__ static constexpr bool aux_own() {
+        return base_bytes<T>() + sizeof(T) * (size_t)NA * QN <=
+               (sizeof(T) == 8 ? (size_t)230000 : (size_t)115000);
+    }
+    template <typename T>
+    __host__ __device__ static constexpr size_t smem_bytes() {
+        return base_bytes<T>() + (aux_own<T>() ? sizeof(T) * (size_t)NA * QN : 0);
     }
 };
 
@@ -215,9 +250,10 @@ __device__ __forceinline__ void phase_aux(const typename RP::Params &P, const T 
     constexpr int M = RP::M, NA = RP::NA;
     if (NA == 0) return;
     // cells the sweep's edges touch: x-sweep cx 0..TX+3, cy 1..TY+2;
-    // y-sweep cx 1..TX+2, cy 0..TY+3
-    constexpr int W = (IXY == 1) ? TX + 4 : TX + 2, H = (IXY == 1) ? TY + 2 : TY + 4;
-    constexpr int X0 = (IXY == 1) ? 0 : 1, Y0 = (IXY == 1) ? 1 : 0;
+    // y-sweep cx 1..TX+2, cy 0..TY+3; IXY = 0: every cell of the tile and
+    // its halo, for both sweeps
+    constexpr int W = (IXY == 2) ? TX + 2 : TX + 4, H = (IXY == 1) ? TY + 2 : TY + 4;
+    constexpr int X0 = (IXY == 2) ? 1 : 0, Y0 = (IXY == 1) ? 1 : 0;
     for (int it = threadIdx.x; it < W * H; it += NT) {
         const int c = (Y0 + it / W) * TL::QW + X0 + it % W;
         T q[M], aux[NA > 0 ? NA : 1];
@@ -262,7 +298,8 @@ __device__ __forceinline__ void phase_rpn2(const typename RP::Params &P, const T
         bad |= RP::template rpn2<IXY>(P, ql, qr, al, ar, W, s, am, ap, R);
 #pragma unroll
         for (int f = 0; f < MW * M; f++)
-            if (RP::template wnz<IXY>(f / M, f % M)) EA[(TL::FW + f) * TL::NE1 + it] = W[f];
+            if (RP::template wnz<IXY>(f / M, f % M))
+                EA[(TL::FW + wave_plane<RP, IXY>(f / M, f % M)) * TL::NE1 + it] = W[f];
 #pragma unroll
         for (int p = 0; p < MW; p++) EA[(TL::FS + p) * TL::NE1 + it] = s[p];
 #pragma unroll
@@ -300,7 +337,9 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
         // stored nor loaded; the sums below then skip exact +0 terms
 #pragma unroll
         for (int f = 0; f < MW * M; f++)
-            W[f] = RP::template wnz<IXY>(f / M, f % M) ? EA[(TL::FW + f) * TL::NE1 + ie] : (T)0;
+            W[f] = RP::template wnz<IXY>(f / M, f % M)
+                       ? EA[(TL::FW + wave_plane<RP, IXY>(f / M, f % M)) * TL::NE1 + ie]
+                       : (T)0;
 #pragma unroll
         for (int p = 0; p < MW; p++) s[p] = EA[(TL::FS + p) * TL::NE1 + ie];
 #pragma unroll
@@ -324,12 +363,14 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
 #pragma unroll
                     for (int k = 0; k < M; k++)
                         if (RP::template wnz<IXY>(p, k))
-                            dot = dot + EA[(TL::FW + p * M + k) * TL::NE1 + ie - STEP] * W[p * M + k];
+                            dot = dot + EA[(TL::FW + wave_plane<RP, IXY>(p, k)) * TL::NE1 + ie - STEP] *
+                                            W[p * M + k];
                 } else {
 #pragma unroll
                     for (int k = 0; k < M; k++)
                         if (RP::template wnz<IXY>(p, k))
-                            dot = dot + W[p * M + k] * EA[(TL::FW + p * M + k) * TL::NE1 + ie + STEP];
+                            dot = dot + W[p * M + k] *
+                                            EA[(TL::FW + wave_plane<RP, IXY>(p, k)) * TL::NE1 + ie + STEP];
                 }
                 const T phi = philim<T>(lim, dot / wn2);
 #pragma unroll
@@ -530,7 +571,9 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, const typename RPT<
     T *QS = reinterpret_cast<T *>(smem_raw);
     T *EA = QS + M * TL::QN;
     T *EB = EA + TL::EAW * TL::NE1;
-    T *CA = EB;
+    constexpr bool AUX1 = TL::template aux_own<T>();  // aux once per tile
+    static_assert(AUX1 || RP::NA * TL::QN <= TL::EBW * TL::NE2, "cell aux area does not fit");
+    T *CA = AUX1 ? EB + TL::EBW * TL::NE2 : EB;
     const T tdtdx = (T)dtdx, tdtdy = (T)dtdy;
 
     load_tile<RP, T, TX, TY, NT>(a, qin, i0, j0, QS);
@@ -546,7 +589,7 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, const typename RPT<
             acc[t][k] = (FP64 && n < TX * TY) ? QS[k * TL::QN + (cj + 2) * TL::QW + ci + 2] : (A)0;
     }
 
-    phase_aux<RP, T, 1, TX, TY, NT>(P, QS, CA);
+    phase_aux<RP, T, AUX1 ? 0 : 1, TX, TY, NT>(P, QS, CA);
     __syncthreads();
     phase_rpn2<RP, T, 1, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, smax_x, bad);
     __syncthreads();
@@ -554,8 +597,10 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, const typename RPT<
     __syncthreads();
     phase_accum<RP, T, A, 1, TX, TY, NT, NC>(EA, EB, acc, tdtdx, tdtdy);
     __syncthreads();
-    phase_aux<RP, T, 2, TX, TY, NT>(P, QS, CA);
-    __syncthreads();
+    if (!AUX1) {
+        phase_aux<RP, T, 2, TX, TY, NT>(P, QS, CA);
+        __syncthreads();
+    }
     phase_rpn2<RP, T, 2, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, smax_y, bad);
     __syncthreads();
     phase_limit<RP, T, 2, TX, TY, NT>(P, EA, EB, a.mthlim, a.order, a.tw, tdtdy);
