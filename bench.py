@@ -64,6 +64,8 @@ def parse_args():
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--batched-steps", type=int, default=200)
     p.add_argument("--no-adjoint", action="store_true")
+    p.add_argument("--no-euler", action="store_true")
+    p.add_argument("--euler-steps", type=int, default=500)
     return p.parse_args()
 
 
@@ -309,6 +311,45 @@ def bench_batched(args, torch, world, device):
             "rel_l1_vs_fp64_max_over_128_problems": max(errs)}
 
 
+def bench_euler(args, torch, world, device):
+    """Four-quadrant Euler problem, 4096^2, superbee, CFL 0.8: FP32-bulk and
+    FP64 step rates over `euler_steps` steps (537 MB per state buffer, above
+    L2, so no flush) and the FP32-bulk error against the FP64 run."""
+    from clawpack_gb300 import workloads
+    from clawpack_gb300.device import DeviceProblem
+
+    n = args.euler_steps
+    small = workloads.euler_quadrants(128, 128, nsteps=3)
+    w = workloads.euler_quadrants(nsteps=n)
+    res, finals = {}, {}
+    for name, prec in (("fp32_bulk", 1), ("fp64", 0)):
+        for prob, steps in ((small, 3), (w, n)):  # the small run loads the kernel
+            dev = DeviceProblem(prob.solver_struct(prec), device=device)
+            dev.upload(prob.q0)
+            dev.ctrl_init(0.0, prob.dt_initial, math.inf, cfl_max=prob.cfl_max,
+                          cfl_desired=prob.cfl_desired, max_accepted=steps, max_steps=10 * steps)
+            torch.cuda.synchronize()
+            barrier(world)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dev.advance(steps)
+            e1.record()
+            torch.cuda.synchronize()
+        secs = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world, device)
+        c = dev.read_ctrl()
+        finals[name] = dev.q[c.parity].clone()
+        res[name] = {"value": round(world * w.mx * w.my * c.numsteps / secs * 1e-9, 4),
+                     "ms_per_step": round(secs / n * 1e3, 4), "accepted_steps": int(c.numsteps),
+                     "attempts": int(c.attempts)}
+        del dev
+    a, b = finals["fp32_bulk"], finals["fp64"]
+    return {"workload": f"euler_quadrants {w.mx}x{w.my} 4-wave Roe + efix, superbee, extrap BCs, "
+                        f"CFL 0.8, {n} steps (seed {w.meta['seed']})",
+            "unit": UNIT, **res,
+            "fp32_rel_l1_vs_fp64": float((a - b).abs().sum() / b.abs().sum()),
+            "launches": 2 * (n + 3)}
+
+
 def bench_adjoint(torch, world, device):
     """Gradient of the gauge least-squares loss with respect to the initial
     surface: 1024^2 shallow water, 500 steps, checkpoints every 23 steps,
@@ -383,9 +424,19 @@ def cpu_baseline(w, target_s=15.0):
         q, cfl, _ = one(q, dt)
     secs = time.perf_counter() - t0
     cells = w.mx * w.my
+    # one thread, as the reference's serial step runs
+    n1, t1 = 0, time.perf_counter()
+    while n1 == 0 or (time.perf_counter() - t1 < target_s / 2 and n1 < 50):
+        q1, cfl1, _ = ref.step(w.rp_id, w.pd_array(), w.q0, w.dx, w.dy, w.dt_initial,
+                               w.bc_lower, w.bc_upper, w.order, w.transverse_waves, w.mthlim(),
+                               nthreads=1)
+        n1 += 1
+    secs1 = time.perf_counter() - t1
     return {"value": cells * n / secs * 1e-9, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{n} full {w.mx}x{w.my} steps of the same problem on {threads} threads "
-                      f"(OpenMP over slices), {secs:.1f} s"}
+                      f"(OpenMP over slices), {secs:.1f} s",
+            "one_thread": {"value": cells * n1 / secs1 * 1e-9, "cores": 1,
+                           "sample": f"{n1} full {w.mx}x{w.my} steps on one thread, {secs1:.1f} s"}}
 
 
 # ------------------------------------------------------------------ arms
@@ -425,7 +476,9 @@ def run_ours(args):
                                "transverse_waves=2, CFL 0.9, FP64",
                    "mx": w.mx, "my": w.my, "accepted_steps": accepted,
                    "l2": "flushed before every timed step (256 MB write, untimed)",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "seeds": {"euler": workloads.EULER_SEED, "batched": workloads.BATCH_SEED,
+                             "adjoint": workloads.ADJOINT_SEED}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": f"{peak_kind} HBM copy bandwidth",
@@ -462,6 +515,9 @@ def run_ours(args):
     if not args.no_batched:
         out["batched"] = bench_batched(args, torch, world, device)
         out["gpu_launches"] += out["batched"]["launches"]
+    if not args.no_euler:
+        out["euler"] = bench_euler(args, torch, world, device)
+        out["gpu_launches"] += out["euler"]["launches"]
     if not args.no_adjoint:
         out["adjoint"] = bench_adjoint(torch, world, device)
         out["gpu_launches"] += out["adjoint"]["launches"]

@@ -489,7 +489,27 @@ struct RpEuler {
         sb[2] = v;
         wb[12] = a4; wb[12 + mu] = a4 * u; wb[12 + mv] = a4 * (v + a); wb[15] = a4 * (enth + v * a);
         sb[3] = v + a;
-        split_sum<T, 4, 4>(sb, wb, bm, bp);
+        if (sb[0] <= (T)0 && sb[3] >= (T)0) {
+            // Subsonic across the edge: the first acoustic wave goes only
+            // down, the second only up; the entropy and shear waves share
+            // speed v.  The terms dropped from split_sum's sums are exact
+            // zeros (including the shear wave's zero density and transverse
+            // momentum).
+            const T m = tmin(v, (T)0), p = tmax(v, (T)0);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                T lo = sb[0] * wb[k] + m * wb[4 + k];
+                T hi = p * wb[4 + k];
+                if (k == mu || k == 3) {
+                    lo = lo + m * wb[8 + k];
+                    hi = hi + p * wb[8 + k];
+                }
+                bm[k] = lo;
+                bp[k] = hi + sb[3] * wb[12 + k];
+            }
+        } else {
+            split_sum<T, 4, 4>(sb, wb, bm, bp);
+        }
     }
 };
 

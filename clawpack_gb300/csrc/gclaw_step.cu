@@ -338,7 +338,10 @@ int gclaw_step_host(const gclaw_solver *s, const double *q_host, double *qnew_ho
     double *d_q = (double *)((char *)ws_dev + 256);
     double *d_new = (double *)((char *)ws_dev + 256 + qpad);
     cudaStream_t st = (cudaStream_t)stream;
-    if (cudaMemcpyAsync(d_q, q_host, qb, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    // the workspace is raw caller memory: clear the control block whose
+    // reduction slots and block counter the step expects at zero
+    if (cudaMemsetAsync(ws, 0, sizeof(gclaw_ctrl), st) != cudaSuccess ||
+        cudaMemcpyAsync(d_q, q_host, qb, cudaMemcpyHostToDevice, st) != cudaSuccess)
         return GCLAW_ERR_CUDA;
     rc = gclaw_step(s, d_q, d_new, dt, ws, stream);
     if (rc) return rc;

@@ -372,7 +372,9 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
                             dot = dot + W[p * M + k] *
                                             EA[(TL::FW + wave_plane<RP, IXY>(p, k)) * TL::NE1 + ie + STEP];
                 }
-                const T phi = philim<T>(lim, dot / wn2);
+                // theta = dot / wn2 <= 0 gives phi = 0 for every limiter id
+                // (1-4), so the quotient is only taken for dot > 0
+                const T phi = (dot <= (T)0) ? (T)0 : philim<T>(lim, dot / wn2);
 #pragma unroll
                 for (int k = 0; k < M; k++) W[p * M + k] = phi * W[p * M + k];
             }

@@ -166,8 +166,8 @@ size_t gclaw_step_workspace_bytes(const gclaw_solver *s);
  * _apply_bcs + step2.  Copies q_host (num_eqn, mx, my) to the device, runs
  * gclaw_step, copies the new state to qnew_host and the Courant number to
  * *cfl_out, then synchronises the stream.  ws_dev (caller-owned, 256-byte
- * aligned, at least gclaw_step_workspace_bytes) holds the control block and
- * both device states. */
+ * aligned, at least gclaw_step_workspace_bytes, any contents) holds the
+ * control block, which each call clears, and both device states. */
 int gclaw_step_host(const gclaw_solver *s, const double *q_host, double *qnew_host, double dt,
                     void *ws_dev, size_t ws_bytes, double *cfl_out, void *stream);
 

@@ -6,7 +6,7 @@ SHAPES = {RP_ACOUSTICS: (3, 2), RP_SHALLOW: (3, 3), RP_EULER: (4, 4)}
 PD = {RP_ACOUSTICS: [1.0, 4.0, 2.0, 2.0], RP_SHALLOW: [1.0], RP_EULER: [1.4, 1.0]}
 
 
-def random_state(rp, mx, my, rng, smooth=False):
+def random_state(rp, mx, my, rng):
     m = SHAPES[rp][0]
     q = np.empty((m, mx, my), order="F")
     if rp == RP_ACOUSTICS:
