@@ -114,6 +114,7 @@ SIGNATURES = {
     "gclaw_evolve_workspace_bytes": (_SZ, [_SP]),
     "gclaw_step2_noalloc": (_I, [_SP, _P, _P, _D, ctypes.POINTER(_D), _P]),
     "gclaw_adjoint_step": (_I, [_SP, _P, _P, _P, _D, _P]),
+    "gclaw_fp32_kernel": (_I, [_I]),
     "gclaw_batch_table_bytes": (_SZ, [_I]),
     "gclaw_batch_prepare": (_I, [_SP, _P, _I, _P, _SZ, ctypes.POINTER(_I), _P]),
     "gclaw_batch_ctrl_init": (_I, [_P, _I, _P, _D, _D, _D, _D, _D, _I, _I, _I, _P]),

@@ -41,7 +41,11 @@ def main(argv=None):
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     p.add_argument("--adjoint", action="store_true")
+    p.add_argument("--fp32-kernel", default="auto", choices=["auto", "tile", "strip"])
     a = p.parse_args(argv)
+    from . import _lib
+
+    _lib.lib().gclaw_fp32_kernel({"auto": 0, "tile": 1, "strip": 2}[a.fp32_kernel])
     w = make_workload(a.workload, a.mx, a.my or a.mx)
     s = w.solver_struct(0 if a.precision == "fp64" else 1)
     dev = DeviceProblem(s)

@@ -130,6 +130,12 @@ int gclaw_ctrl_init(gclaw_ctrl *ctrl_dev, double t, double dt, double t_end, dou
                     double cfl_desired, double dt_max, int max_steps, int max_accepted,
                     int dt_variable, void *stream);
 
+/* Kernel family of the FP32-bulk step, for the whole process: 0 = the
+ * per-solver default, 1 = shared-memory tiles, 2 = register strips (one
+ * warp per 28-column strip marching up its rows).  Both compute the same
+ * step; any other value only queries.  Returns the previous setting. */
+int gclaw_fp32_kernel(int which);
+
 /* Drop-in for classic2.step2 (upstream pyclaw/src/pyclaw/classic/step2.f90):
  * one unsplit step of a ghost-filled qbc.  qold_dev and qnew_dev are
  * (num_eqn, mx+4, my+4) Fortran order; the interior of qnew_dev receives the
