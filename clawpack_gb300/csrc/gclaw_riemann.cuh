@@ -43,6 +43,90 @@ __device__ __forceinline__ float tmin<float>(float a, float b) { return fminf(a,
 template <>
 __device__ __forceinline__ float tmax<float>(float a, float b) { return fmaxf(a, b); }
 
+// Tests of a value against zero with IEEE results (NaN compares false,
+// -0 == +0), and min / max of values known to be in [+0, +inf].  For
+// doubles they are integer tests on the bit pattern: GB300 executes FP64
+// comparisons, min and max on its FP64 pipe, which is the unit the FP64
+// step is bound by, while the integer pipes are idle.
+template <typename T>
+__device__ __forceinline__ bool gt0(T x) { return x > (T)0; }
+template <typename T>
+__device__ __forceinline__ bool lt0(T x) { return x < (T)0; }
+template <typename T>
+__device__ __forceinline__ bool isnan_v(T x) { return x != x; }
+template <typename T>
+__device__ __forceinline__ T nnmin(T a, T b) { return tmin(a, b); }
+template <typename T>
+__device__ __forceinline__ T nnmax(T a, T b) { return tmax(a, b); }
+
+constexpr long long F64_INF_BITS = 0x7FF0000000000000LL;
+constexpr long long F64_ABS_MASK = 0x7FFFFFFFFFFFFFFFLL;
+template <>
+__device__ __forceinline__ bool gt0<double>(double x) {
+    const long long b = __double_as_longlong(x);
+    return b > 0 && b <= F64_INF_BITS;  // sign clear, not +0, not NaN
+}
+template <>
+__device__ __forceinline__ bool lt0<double>(double x) {
+    const long long b = __double_as_longlong(x);
+    const unsigned long long m = (unsigned long long)(b & F64_ABS_MASK);
+    return b < 0 && m - 1ull < (unsigned long long)F64_INF_BITS;  // sign set, 0 < |x| <= inf
+}
+template <>
+__device__ __forceinline__ bool isnan_v<double>(double x) {
+    return (__double_as_longlong(x) & F64_ABS_MASK) > F64_INF_BITS;
+}
+template <>
+__device__ __forceinline__ double nnmin<double>(double a, double b) {
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return __longlong_as_double(x < y ? x : y);
+}
+template <>
+__device__ __forceinline__ double nnmax<double>(double a, double b) {
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return __longlong_as_double(x > y ? x : y);
+}
+// a < b and a >= b (IEEE) when b is in [+0, +inf] and a is >= +0, -0 or NaN
+template <typename T>
+__device__ __forceinline__ bool nn_lt(T a, T b) { return a < b; }
+template <typename T>
+__device__ __forceinline__ bool nn_ge(T a, T b) { return a >= b; }
+template <>
+__device__ __forceinline__ bool nn_lt<double>(double a, double b) {
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return y <= F64_INF_BITS && x < y;
+}
+template <>
+__device__ __forceinline__ bool nn_ge<double>(double a, double b) {
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return x <= F64_INF_BITS && x >= y;
+}
+template <typename T>
+__device__ __forceinline__ bool ge0(T x) { return !lt0(x) && !isnan_v(x); }
+template <typename T>
+__device__ __forceinline__ bool eq0(T x) { return x == (T)0; }
+template <>
+__device__ __forceinline__ bool eq0<double>(double x) {
+    return (__double_as_longlong(x) & F64_ABS_MASK) == 0;
+}
+template <typename T>
+__device__ __forceinline__ bool le0(T x) { return !gt0(x) && !isnan_v(x); }
+// min(x, 0) and max(x, 0) as fmin / fmax give them (NaN -> 0), by sign
+template <typename T>
+__device__ __forceinline__ T neg_part(T x) { return lt0(x) ? x : (T)0; }
+template <typename T>
+__device__ __forceinline__ T pos_part(T x) { return gt0(x) ? x : (T)0; }
+
+// Running max of |s| over non-NaN speeds, as fmax(m, fabs(s)) gives it.
+template <typename T>
+__device__ __forceinline__ T max_abs(T m, T s) { return tmax(m, (T)fabs(s)); }
+template <>
+__device__ __forceinline__ double max_abs<double>(double m, double s) {
+    const long long a = __double_as_longlong(s) & F64_ABS_MASK;
+    const long long b = __double_as_longlong(m);
+    return a <= F64_INF_BITS && a > b ? __longlong_as_double(a) : m;
+}
+
 // True when fl(m / h - sqrt(g h)) > 0 cannot hold, decided without the
 // division and the square root: h > 0 and either m <= 0 (the quotient is
 // not positive) or m^2 < 0.81 g h^3 (|m / h| < 0.9 sqrt(g h) exactly, a
@@ -53,10 +137,11 @@ __device__ __forceinline__ float tmax<float>(float a, float b) { return fmaxf(a,
 // certain to fail (every subsonic edge), with unchanged branch decisions.
 template <typename T>
 __device__ __forceinline__ bool no_right_sonic_point(T h, T m, T g) {
-    if (!(h > (T)0)) return false;
-    if (m <= (T)0) return true;
+    if (!gt0(h)) return false;
+    if (le0(m)) return true;
     const T rhs = (T)0.81 * g * h * h * h;
-    return rhs >= (sizeof(T) == 8 ? (T)1e-290 : (T)1e-30) && m * m < rhs;
+    const T tiny = sizeof(T) == 8 ? (T)1e-290 : (T)1e-30;
+    return nn_ge(rhs, tiny) && nn_lt(m * m, rhs);
 }
 
 // ---------------------------------------------------------------------------
@@ -116,8 +201,8 @@ __device__ __forceinline__ void split_sum(const T *sb, const T *wb, T *bm, T *bp
         T lo = (T)0, hi = (T)0;
 #pragma unroll
         for (int p = 0; p < MW; p++) {
-            lo = lo + tmin(sb[p], (T)0) * wb[M * p + k];
-            hi = hi + tmax(sb[p], (T)0) * wb[M * p + k];
+            lo = lo + neg_part(sb[p]) * wb[M * p + k];
+            hi = hi + pos_part(sb[p]) * wb[M * p + k];
         }
         bm[k] = lo;
         bp[k] = hi;
@@ -223,7 +308,7 @@ struct RpShallow {
 
         // entropy fix: amdq first, apdq = sum(s W) - amdq
         const T s0 = al[2 + mu] - al[5];  // u - c in the left cell
-        if (s0 >= (T)0 && s[0] > (T)0) {
+        if (ge0(s0) && gt0(s[0])) {
 #pragma unroll
             for (int k = 0; k < 3; k++) am[k] = (T)0;
         } else {
@@ -231,19 +316,19 @@ struct RpShallow {
             T hu1 = ql[mu] + w1[mu];
             T s1 = (T)0, sfract;
             bool sonic1 = false;  // s0 < 0 < s1: transonic 1-rarefaction
-            if (s0 < (T)0 && !no_right_sonic_point(h1, hu1, g)) {
+            if (lt0(s0) && !no_right_sonic_point(h1, hu1, g)) {
                 s1 = hu1 / h1 - sqrt(g * h1);
                 sonic1 = s1 > (T)0;
             }
             if (sonic1)
                 sfract = s0 * (s1 - s[0]) / (s1 - s0);
-            else if (s[0] < (T)0)
+            else if (lt0(s[0]))
                 sfract = s[0];
             else
                 sfract = (T)0;
 #pragma unroll
             for (int k = 0; k < 3; k++) am[k] = sfract * w1[k];
-            if (s[1] < (T)0) {
+            if (lt0(s[1])) {
 #pragma unroll
                 for (int k = 0; k < 3; k++) am[k] = am[k] + s[1] * w2[k];
                 const T s03 = ar[2 + mu] + ar[5];  // u + c in the right cell
@@ -251,14 +336,14 @@ struct RpShallow {
                 T hu3 = qr[mu] - w3[mu];
                 T s3 = (T)0;
                 bool sonic3 = false;  // s3 < 0 < s03: transonic 3-rarefaction
-                if (s03 > (T)0 && !no_right_sonic_point(h3, -hu3, g)) {
+                if (gt0(s03) && !no_right_sonic_point(h3, -hu3, g)) {
                     s3 = hu3 / h3 + sqrt(g * h3);
                     sonic3 = s3 < (T)0;
                 }
                 bool add = true;
                 if (sonic3)
                     sfract = s3 * (s03 - s[2]) / (s03 - s3);
-                else if (s[2] < (T)0)
+                else if (lt0(s[2]))
                     sfract = s[2];
                 else
                     add = false;
@@ -293,12 +378,12 @@ struct RpShallow {
         sb[1] = vbar;
         wb[6] = a3; wb[6 + mu] = a3 * ubar; wb[6 + mv] = a3 * (vbar + cbar);
         sb[2] = vbar + cbar;
-        if (sb[0] <= (T)0 && sb[2] >= (T)0) {
+        if (le0(sb[0]) && ge0(sb[2])) {
             // Subsonic across the edge (the usual case): the first wave
             // goes only down, the third only up, and the shear wave has
             // one component, so the sums of split_sum reduce to these
             // terms; the dropped terms are exact zeros.
-            const T m1 = tmin(sb[1], (T)0), p1 = tmax(sb[1], (T)0);
+            const T m1 = neg_part(sb[1]), p1 = pos_part(sb[1]);
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 bm[k] = sb[0] * wb[k];
@@ -489,13 +574,13 @@ struct RpEuler {
         sb[2] = v;
         wb[12] = a4; wb[12 + mu] = a4 * u; wb[12 + mv] = a4 * (v + a); wb[15] = a4 * (enth + v * a);
         sb[3] = v + a;
-        if (sb[0] <= (T)0 && sb[3] >= (T)0) {
+        if (le0(sb[0]) && ge0(sb[3])) {
             // Subsonic across the edge: the first acoustic wave goes only
             // down, the second only up; the entropy and shear waves share
             // speed v.  The terms dropped from split_sum's sums are exact
             // zeros (including the shear wave's zero density and transverse
             // momentum).
-            const T m = tmin(v, (T)0), p = tmax(v, (T)0);
+            const T m = neg_part(v), p = pos_part(v);
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 T lo = sb[0] * wb[k] + m * wb[4 + k];
@@ -523,6 +608,23 @@ __device__ __forceinline__ T philim(int id, T r) {
     case 4: {
         T c = ((T)1 + r) / (T)2;
         return tmax((T)0, tmin(c, tmin((T)2, (T)2 * r)));
+    }
+    default: return (T)1;
+    }
+}
+
+// philim for theta in (0, +inf]: every operand of the min / max is then in
+// [+0, +inf] and the outer max with 0 is the identity, so the same values
+// come from nnmin / nnmax.
+template <typename T>
+__device__ __forceinline__ T philim_pos(int id, T r) {
+    switch (id) {
+    case 1: return nnmin((T)1, r);
+    case 2: return nnmax(nnmin((T)1, (T)2 * r), nnmin((T)2, r));
+    case 3: return (r + r) / ((T)1 + r);
+    case 4: {
+        T c = ((T)1 + r) / (T)2;
+        return nnmin(c, nnmin((T)2, (T)2 * r));
     }
     default: return (T)1;
     }

@@ -313,8 +313,8 @@ __device__ __forceinline__ void phase_rpn2(const typename RP::Params &P, const T
         if (ea >= 1 && ea <= NA1 - 2 && ge <= n && gs <= nt) {
 #pragma unroll
             for (int p = 0; p < MW; p++) {
-                bad |= (s[p] != s[p]);
-                smax = tmax(smax, (T)fabs(s[p]));
+                bad |= isnan_v(s[p]);
+                smax = max_abs(smax, s[p]);
             }
         }
     }
@@ -357,9 +357,9 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
 #pragma unroll
                 for (int k = 0; k < M; k++)
                     if (RP::template wnz<IXY>(p, k)) wn2 = wn2 + W[p * M + k] * W[p * M + k];
-                if (wn2 == (T)0) continue;
+                if (eq0(wn2)) continue;
                 T dot = (T)0;
-                if (s[p] > (T)0) {
+                if (gt0(s[p])) {
 #pragma unroll
                     for (int k = 0; k < M; k++)
                         if (RP::template wnz<IXY>(p, k))
@@ -374,7 +374,11 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
                 }
                 // theta = dot / wn2 <= 0 gives phi = 0 for every limiter id
                 // (1-4), so the quotient is only taken for dot > 0
-                const T phi = (dot <= (T)0) ? (T)0 : philim<T>(lim, dot / wn2);
+                T phi = (T)0;
+                if (!le0(dot)) {
+                    const T th = dot / wn2;
+                    phi = gt0(th) ? philim_pos<T>(lim, th) : philim<T>(lim, th);
+                }
 #pragma unroll
                 for (int k = 0; k < M; k++) W[p * M + k] = phi * W[p * M + k];
             }
