@@ -3,8 +3,10 @@ pyclaw/src/pyclaw/controller.py; absent from the mounted tree).
 
 output_style 1: frames at num_output_times equally spaced times from the
 initial time to tfinal; output_style 2: the times in ``out_times``.  Frames are
-kept in memory (``keep_copy``); writing them to disk is not part of this
-package.
+kept in memory (``keep_copy``) and, when ``output_format`` is 'ascii' or
+'binary', written to ``outdir`` as ``<output_file_prefix>.t/q/bNNNN`` (frame 0
+is the initial state).  ``output_format`` defaults to None (no files), since
+ascii frames of large grids take far longer to write than to compute.
 """
 from __future__ import annotations
 
@@ -23,6 +25,9 @@ class Controller:
         self.out_times = None
         self.keep_copy = True
         self.output_format = None
+        self.outdir = "./_output"
+        self.output_file_prefix = None
+        self.output_options = {}
         self.frames = []
         self.logger = logging.getLogger("pyclaw.controller")
 
@@ -38,12 +43,17 @@ class Controller:
             raise NotImplementedError("output_style must be 1 or 2")
         self.solver.setup(self.solution)
         self.frames = []
-        if self.keep_copy:
-            self.frames.append(self.solution.copy())
+        self._output(0)
         status = self.solver.status
         for k, t_out in enumerate(times[1:], start=1):
             status = self.solver.evolve_to_time(self.solution, t_out)
-            if self.keep_copy:
-                self.frames.append(self.solution.copy())
+            self._output(k)
             self.logger.info("Solution %d computed for time t=%f", k, self.solution.t)
         return status
+
+    def _output(self, frame):
+        if self.keep_copy:
+            self.frames.append(self.solution.copy())
+        if self.output_format is not None:
+            self.solution.write(frame, self.outdir, self.output_format, self.output_file_prefix,
+                                options=self.output_options)

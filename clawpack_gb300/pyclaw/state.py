@@ -42,12 +42,36 @@ class State:
 
 
 class Solution:
-    """``Solution(state, domain)``; ``solution.t`` is the time of the state."""
+    """``Solution(state, domain)``, or ``Solution(frame, path=..., file_format=...,
+    file_prefix=...)`` to load an output frame; ``solution.t`` is the time
+    of the state."""
 
-    def __init__(self, state, domain=None):
-        self.states = [state]
+    def __init__(self, state, domain=None, path="./_output", file_format="ascii",
+                 file_prefix=None):
+        self.states = []
         self.domain = domain
         self.t = 0.0
+        if isinstance(state, (int, np.integer)):
+            self.read(int(state), path, file_format, file_prefix)
+        else:
+            self.states = [state]
+
+    def write(self, frame, path="./", file_format="ascii", file_prefix=None, write_aux=False,
+              options=None, write_p=False):
+        """Write this solution as output frame ``frame`` (formats 'ascii' and
+        'binary', see clawpack_gb300.pyclaw.fileio)."""
+        from . import fileio
+
+        fileio.module(file_format).write(self, frame, path, file_prefix or "fort", write_aux,
+                                         options or {}, write_p)
+
+    def read(self, frame, path="./_output", file_format="ascii", file_prefix=None,
+             read_aux=False, options=None):
+        """Replace this solution's state by output frame ``frame``."""
+        from . import fileio
+
+        return fileio.module(file_format).read(self, frame, path, file_prefix or "fort",
+                                               read_aux, options or {})
 
     @property
     def state(self):
