@@ -115,6 +115,8 @@ SIGNATURES = {
     "gclaw_step2_noalloc": (_I, [_SP, _P, _P, _D, ctypes.POINTER(_D), _P]),
     "gclaw_adjoint_step": (_I, [_SP, _P, _P, _P, _D, _P]),
     "gclaw_fp32_kernel": (_I, [_I]),
+    "gclaw_step_split": (_I, [_SP, _P, _P, _P, _D, _P, _P]),
+    "gclaw_advance_split": (_I, [_SP, _P, _P, _P, _P, _I, _P]),
     "gclaw_batch_table_bytes": (_SZ, [_I]),
     "gclaw_batch_prepare": (_I, [_SP, _P, _I, _P, _SZ, ctypes.POINTER(_I), _P]),
     "gclaw_batch_ctrl_init": (_I, [_P, _I, _P, _D, _D, _D, _D, _D, _I, _I, _I, _P]),

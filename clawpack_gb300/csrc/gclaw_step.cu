@@ -81,7 +81,8 @@ __global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1) step_kernel(const StepA
         const unsigned prev = atomicAdd(&c->blocks_done, 1u);
         if (prev == nblocks - 1) {
             __threadfence();
-            finish_step(c, a.ctrl_mode, dt, dtdx, dtdy);
+            if (a.no_finish) c->blocks_done = 0u;
+            else finish_step(c, a.ctrl_mode, dt, dtdx, dtdy);
         }
     }
 }
@@ -253,7 +254,9 @@ bool strip_default<RpEuler>() { return false; }
 template <template <typename> class RPT, typename T>
 static int launch_cfg(const gclaw_solver *s, const StepArgs &a, cudaStream_t st, int nlaunch) {
     using C = TileCfg<RPT, T>;
-    if (sizeof(T) == 4 && (g_fp32_kernel == 2 || (g_fp32_kernel == 0 && strip_default<RPT>())))
+    const bool split = a.sweeps == 1 || a.sweeps == 2;  // strips run both sweeps at once
+    if (sizeof(T) == 4 && !split &&
+        (g_fp32_kernel == 2 || (g_fp32_kernel == 0 && strip_default<RPT>())))
         return launch_strip<RPT>(s, a, st, nlaunch);
     return launch_tile<RPT, T, C::TX, C::TY, C::NT>(s, a, st, nlaunch);
 }
@@ -434,6 +437,64 @@ int gclaw_advance(const gclaw_solver *s, double *q0_dev, double *q1_dev, gclaw_c
     a.ghosted = 0;
     a.ctrl_mode = 1;
     return dispatch(s, a, (cudaStream_t)stream, nlaunch);
+}
+
+// Dimensionally split step: the x-sweep from qin into qtmp (its last block
+// keeps the CFL reduction open), then the y-sweep from qtmp into qout, whose
+// last block finishes the step with both sweeps' max |s|.
+static int dispatch_split(const gclaw_solver *s, StepArgs ax, cudaStream_t st, int nsteps,
+                          double *qtmp) {
+    StepArgs ay = ax;
+    ax.sweeps = 1;
+    ax.no_finish = 1;
+    ax.tw = 0;
+    ax.qout[0] = ax.qout[1] = qtmp;
+    ay.sweeps = 2;
+    ay.no_finish = 0;
+    ay.tw = 0;
+    ay.qin[0] = ay.qin[1] = qtmp;
+    for (int l = 0; l < nsteps; l++) {
+        int rc = dispatch(s, ax, st, 1);
+        if (rc == GCLAW_OK) rc = dispatch(s, ay, st, 1);
+        if (rc != GCLAW_OK) return rc;
+    }
+    return GCLAW_OK;
+}
+
+int gclaw_step_split(const gclaw_solver *s, const double *q_dev, double *qnew_dev,
+                     double *qtmp_dev, double dt, gclaw_ctrl *ws_dev, void *stream) {
+    int rc = gclaw_check(s);
+    if (rc) return rc;
+    if (!q_dev || !qnew_dev || !qtmp_dev || !ws_dev || !(dt > 0.0)) return GCLAW_ERR_ARG;
+    if (qtmp_dev == q_dev || qtmp_dev == qnew_dev || q_dev == qnew_dev) return GCLAW_ERR_ARG;
+    StepArgs a{};
+    fill_args(s, a);
+    a.qin[0] = a.qin[1] = q_dev;
+    a.qout[0] = a.qout[1] = qnew_dev;
+    a.ctrl = ws_dev;
+    a.dt = dt;
+    a.ghosted = 0;
+    a.ctrl_mode = 0;
+    return dispatch_split(s, a, (cudaStream_t)stream, 1, qtmp_dev);
+}
+
+int gclaw_advance_split(const gclaw_solver *s, double *q0_dev, double *q1_dev, double *qtmp_dev,
+                        gclaw_ctrl *ctrl_dev, int nsteps, void *stream) {
+    int rc = gclaw_check(s);
+    if (rc) return rc;
+    if (!q0_dev || !q1_dev || !qtmp_dev || !ctrl_dev || nsteps < 0) return GCLAW_ERR_ARG;
+    if (qtmp_dev == q0_dev || qtmp_dev == q1_dev || q0_dev == q1_dev) return GCLAW_ERR_ARG;
+    StepArgs a{};
+    fill_args(s, a);
+    a.qin[0] = q0_dev;
+    a.qin[1] = q1_dev;
+    a.qout[0] = q1_dev;
+    a.qout[1] = q0_dev;
+    a.ctrl = ctrl_dev;
+    a.dt = 0.0;
+    a.ghosted = 0;
+    a.ctrl_mode = 1;
+    return dispatch_split(s, a, (cudaStream_t)stream, nsteps, qtmp_dev);
 }
 
 size_t gclaw_step_workspace_bytes(const gclaw_solver *s) {

@@ -24,6 +24,9 @@ struct StepArgs {
     int bc_lo[2], bc_hi[2];
     int mthlim;  // limiter id of wave p in bits 8p..8p+7
     int order, tw;
+    int sweeps;     // 1: x-sweep only, 2: y-sweep only (dimensional splitting); else both
+    int no_finish;  // last block resets the block counter but leaves the CFL
+                    // reduction to the next launch (first sweep of a split step)
 };
 
 // Value of component k of qbc(gi, gj) for gi in [-2, mx+1], gj in [-2, my+1]
@@ -595,23 +598,36 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, const typename RPT<
             acc[t][k] = (FP64 && n < TX * TY) ? QS[k * TL::QN + (cj + 2) * TL::QW + ci + 2] : (A)0;
     }
 
-    phase_aux<RP, T, AUX1 ? 0 : 1, TX, TY, NT>(P, QS, CA);
-    __syncthreads();
-    phase_rpn2<RP, T, 1, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, smax_x, bad);
-    __syncthreads();
-    phase_limit<RP, T, 1, TX, TY, NT>(P, EA, EB, a.mthlim, a.order, a.tw, tdtdx);
-    __syncthreads();
-    phase_accum<RP, T, A, 1, TX, TY, NT, NC>(EA, EB, acc, tdtdx, tdtdy);
-    __syncthreads();
-    if (!AUX1) {
-        phase_aux<RP, T, 2, TX, TY, NT>(P, QS, CA);
+    // both sweeps (the unsplit step), or one of them (a dimensionally split
+    // step runs them as two launches, x first, with transverse_waves 0)
+    const bool do_x = a.sweeps != 2, do_y = a.sweeps != 1;
+    if (AUX1) {
+        phase_aux<RP, T, 0, TX, TY, NT>(P, QS, CA);
         __syncthreads();
     }
-    phase_rpn2<RP, T, 2, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, smax_y, bad);
-    __syncthreads();
-    phase_limit<RP, T, 2, TX, TY, NT>(P, EA, EB, a.mthlim, a.order, a.tw, tdtdy);
-    __syncthreads();
-    phase_accum<RP, T, A, 2, TX, TY, NT, NC>(EA, EB, acc, tdtdy, tdtdx);
+    if (do_x) {
+        if (!AUX1) {
+            phase_aux<RP, T, 1, TX, TY, NT>(P, QS, CA);
+            __syncthreads();
+        }
+        phase_rpn2<RP, T, 1, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, smax_x, bad);
+        __syncthreads();
+        phase_limit<RP, T, 1, TX, TY, NT>(P, EA, EB, a.mthlim, a.order, a.tw, tdtdx);
+        __syncthreads();
+        phase_accum<RP, T, A, 1, TX, TY, NT, NC>(EA, EB, acc, tdtdx, tdtdy);
+        if (do_y) __syncthreads();
+    }
+    if (do_y) {
+        if (!AUX1) {
+            phase_aux<RP, T, 2, TX, TY, NT>(P, QS, CA);
+            __syncthreads();
+        }
+        phase_rpn2<RP, T, 2, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, smax_y, bad);
+        __syncthreads();
+        phase_limit<RP, T, 2, TX, TY, NT>(P, EA, EB, a.mthlim, a.order, a.tw, tdtdy);
+        __syncthreads();
+        phase_accum<RP, T, A, 2, TX, TY, NT, NC>(EA, EB, acc, tdtdy, tdtdx);
+    }
 
     const int onx = a.ghosted ? a.mx + 4 : a.mx, ooff = a.ghosted ? 2 : 0;
 #pragma unroll

@@ -42,9 +42,11 @@ def make_solver_struct(rp_id, mx, my, dx, dy, bc_lower, bc_upper, mthlim, order,
 
 
 class DeviceProblem:
-    """Two state buffers + control block on one CUDA device."""
+    """Two state buffers + control block on one CUDA device.  With
+    ``split=True`` steps are dimensionally split (x-sweep, then y-sweep) and a
+    third buffer holds the state between the sweeps."""
 
-    def __init__(self, solver_struct, device=None, strict=False):
+    def __init__(self, solver_struct, device=None, strict=False, split=False):
         self.s = solver_struct
         self.L = L = _lib.lib(strict)
         _lib.check(L.gclaw_check(ctypes.byref(self.s)), "gclaw_check")
@@ -57,6 +59,9 @@ class DeviceProblem:
         shape = (self.my, self.mx, self.m)
         self.q = [torch.empty(shape, dtype=torch.float64, device=self.device),
                   torch.empty(shape, dtype=torch.float64, device=self.device)]
+        self.split = bool(split)
+        self.qtmp = (torch.empty(shape, dtype=torch.float64, device=self.device)
+                     if self.split else None)
         self.ctrl = torch.zeros(256, dtype=torch.uint8, device=self.device)
         self._ctrl_host = torch.empty(256, dtype=torch.uint8, pin_memory=True)
         self.ctrl_init(0.0, 1.0, 0.0)
@@ -92,6 +97,13 @@ class DeviceProblem:
     # -- stepping ------------------------------------------------------------
     def advance(self, nlaunch, stream=None):
         """Enqueue ``nlaunch`` controlled steps (no synchronisation)."""
+        if self.split:
+            _lib.check(self.L.gclaw_advance_split(
+                ctypes.byref(self.s), ctypes.c_void_p(self.q[0].data_ptr()),
+                ctypes.c_void_p(self.q[1].data_ptr()), ctypes.c_void_p(self.qtmp.data_ptr()),
+                ctypes.c_void_p(self.ctrl.data_ptr()), int(nlaunch), _stream_handle(stream)),
+                "gclaw_advance_split")
+            return
         _lib.check(self.L.gclaw_advance(
             ctypes.byref(self.s), ctypes.c_void_p(self.q[0].data_ptr()),
             ctypes.c_void_p(self.q[1].data_ptr()), ctypes.c_void_p(self.ctrl.data_ptr()),
@@ -100,6 +112,14 @@ class DeviceProblem:
     def step(self, dt, src=0, stream=None):
         """One step with explicit dt from buffer ``src`` into ``1 - src``; the
         Courant number is left in the control block (see ``read_ctrl``)."""
+        if self.split:
+            _lib.check(self.L.gclaw_step_split(
+                ctypes.byref(self.s), ctypes.c_void_p(self.q[src].data_ptr()),
+                ctypes.c_void_p(self.q[1 - src].data_ptr()),
+                ctypes.c_void_p(self.qtmp.data_ptr()), float(dt),
+                ctypes.c_void_p(self.ctrl.data_ptr()), _stream_handle(stream)),
+                "gclaw_step_split")
+            return
         _lib.check(self.L.gclaw_step(
             ctypes.byref(self.s), ctypes.c_void_p(self.q[src].data_ptr()),
             ctypes.c_void_p(self.q[1 - src].data_ptr()), float(dt),

@@ -9,6 +9,9 @@ meson.build:64): ``rp``, ``limiters``, ``order``, ``transverse_waves``,
 ``num_ghost``, ``step()``, ``evolve_to_time()``, ``status``, ``cfl``.
 
 The step itself runs in libgclaw.so on the GPU; there is no CPU path.  With
+``dimensional_split = True`` (PyClaw's default) takes Godunov-split steps,
+an x-sweep and then a y-sweep without transverse waves
+(``transverse_waves`` is ignored); ``False`` takes the unsplit step.  With
 ``device_control = True`` (default) the evolve_to_time loop (dt choice, CFL
 rejection, landing on tend) runs on the device as well, so the host only
 waits once per batch of ``batch`` step launches.
@@ -125,10 +128,6 @@ class ClawSolver2D:
             raise NotImplementedError(
                 f"kernel_language={self.kernel_language!r}: this framework provides the 'CUDA' "
                 "backend only")
-        if self.dimensional_split:
-            raise NotImplementedError(
-                "dimensional_split=True is not implemented; set solver.dimensional_split = False "
-                "for the unsplit classic step")
         if self.fwave or self.step_source is not None or self.before_step is not None:
             raise NotImplementedError("fwave, step_source and before_step are not supported")
         if self.num_ghost != 2:
@@ -162,9 +161,10 @@ class ClawSolver2D:
 
     def _device(self, state):
         s = self.solver_struct(state)
-        key = bytes(s)
+        split = bool(self.dimensional_split)
+        key = (bytes(s), split)
         if self._dev is None or self._dev_key != key:
-            self._dev = DeviceProblem(s)
+            self._dev = DeviceProblem(s, split=split)
             self._dev_key = key
         return self._dev
 

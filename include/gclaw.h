@@ -163,6 +163,24 @@ int gclaw_step(const gclaw_solver *s, const double *q_dev, double *qnew_dev, dou
 int gclaw_advance(const gclaw_solver *s, double *q0_dev, double *q1_dev, gclaw_ctrl *ctrl_dev,
                   int nlaunch, void *stream);
 
+/* Dimensionally split step (Godunov splitting), the path of
+ * ClawSolver2D.step() with dimensional_split=True (upstream
+ * pyclaw/src/pyclaw/classic/solver.py calling classic2.step2ds with ixy=1,
+ * then with ixy=2 after re-applying the boundary conditions): the x-sweep
+ * of q_dev into qtmp_dev, then the y-sweep of qtmp_dev, with boundary
+ * conditions applied to each input, into qnew_dev; no transverse waves.
+ * The Courant number, the max of both sweeps', is left in ws_dev->cfl.
+ * The three arrays are (num_eqn, mx, my) and distinct. */
+int gclaw_step_split(const gclaw_solver *s, const double *q_dev, double *qnew_dev,
+                     double *qtmp_dev, double dt, gclaw_ctrl *ws_dev, void *stream);
+
+/* gclaw_advance with dimensionally split steps: each of the nsteps steps is
+ * two launches (x-sweep into qtmp_dev, y-sweep into the other state
+ * buffer); the evolve_to_time rules apply to the whole step, so a rejected
+ * step leaves q{parity} unchanged. */
+int gclaw_advance_split(const gclaw_solver *s, double *q0_dev, double *q1_dev, double *qtmp_dev,
+                        gclaw_ctrl *ctrl_dev, int nsteps, void *stream);
+
 /* Device bytes gclaw_step_host needs in ws_dev. */
 size_t gclaw_step_workspace_bytes(const gclaw_solver *s);
 

@@ -641,9 +641,35 @@ double gclaw_ref_philim(int id, double r) { return philim(id, r); }
  * pd: problem data (acoustics: rho, bulk, cc, zz; shallow: grav;
  * euler: gamma, efix).  Returns 0, or ERR_NONPHYSICAL if a Riemann problem
  * met a non-physical state. */
+static int step2_dirs(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
+                      double *qnew, double dx, double dy, double dt, int order, int tw,
+                      const int *mthlim, double *cfl_out, int nthreads, int ixy_lo,
+                      int ixy_hi);
+
 int gclaw_ref_step2(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
                     double *qnew, double dx, double dy, double dt, int order, int tw,
                     const int *mthlim, double *cfl_out, int nthreads)
+{
+    return step2_dirs(rp_id, pd, g, mx, my, qold, qnew, dx, dy, dt, order, tw, mthlim, cfl_out,
+                      nthreads, 1, 2);
+}
+
+/* One sweep of PyClaw's dimensionally split step (classic2 step2ds,
+ * upstream pyclaw/src/pyclaw/classic/step2ds.f90): the slices of direction
+ * ixy only, without transverse propagation, from the ghost-filled qold into
+ * qnew (same shapes as step2).  *cfl_out is that sweep's Courant number. */
+int gclaw_ref_step2ds(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
+                      double *qnew, double dx, double dy, double dt, int order,
+                      const int *mthlim, int ixy, double *cfl_out, int nthreads)
+{
+    if (ixy != 1 && ixy != 2) return ERR_ARG;
+    return step2_dirs(rp_id, pd, g, mx, my, qold, qnew, dx, dy, dt, order, 0, mthlim, cfl_out,
+                      nthreads, ixy, ixy);
+}
+
+static int step2_dirs(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
+                      double *qnew, double dx, double dy, double dt, int order, int tw,
+                      const int *mthlim, double *cfl_out, int nthreads, int ixy_lo, int ixy_hi)
 {
     rp_t rp;
     rp.id = rp_id;
@@ -674,7 +700,7 @@ int gclaw_ref_step2(int rp_id, const double *pd, int g, int mx, int my, const do
     int bad = 0;
     double cfl = 0.0;
 
-    for (int ixy = 1; ixy <= 2; ixy++) {
+    for (int ixy = ixy_lo; ixy <= ixy_hi; ixy++) {
         const int n = (ixy == 1) ? mx : my;
         const int ns = (ixy == 1) ? nslx : nsly;
         const double dtdn = (ixy == 1) ? dtdx : dtdy;
@@ -766,4 +792,47 @@ int gclaw_ref_step(int rp_id, const double *pd, int mx, int my, const double *q,
     free(qa);
     free(qb);
     return rc;
+}
+
+/* PyClaw's dimensionally split step (Godunov splitting, ClawSolver2D with
+ * dimensional_split=True, upstream pyclaw/src/pyclaw/classic/solver.py):
+ * boundary conditions, the x-sweep, boundary conditions again on its
+ * result, the y-sweep; *cfl_out = max of the two sweeps' Courant numbers.
+ * Interior-shaped arrays (m, mx, my). */
+int gclaw_ref_step_split(int rp_id, const double *pd, int mx, int my, const double *q,
+                         double *qout, double dx, double dy, double dt, int order,
+                         const int *mthlim, const int *bc_lower, const int *bc_upper,
+                         double *cfl_out, int nthreads)
+{
+    int m, mw;
+    if (rp_shape(rp_id, &m, &mw)) return ERR_ARG;
+    const int g = 2, nx = mx + 4, ny = my + 4;
+    size_t nb = (size_t)m * nx * ny;
+    double *qa = malloc(sizeof(double) * nb), *qb = malloc(sizeof(double) * nb);
+    double *qi = malloc(sizeof(double) * (size_t)m * mx * my);
+    if (!qa || !qb || !qi) {
+        free(qa); free(qb); free(qi);
+        return ERR_ALLOC;
+    }
+    double cfl[2] = {0.0, 0.0};
+    int rc = 0, bad = 0;
+    const double *src = q;
+    for (int ixy = 1; ixy <= 2 && (rc == 0 || rc == ERR_NONPHYSICAL); ixy++) {
+        rc = gclaw_ref_fill_ghosts(m, mx, my, g, bc_lower, bc_upper, src, qa);
+        if (rc) break;
+        rc = gclaw_ref_step2ds(rp_id, pd, g, mx, my, qa, qb, dx, dy, dt, order, mthlim, ixy,
+                               &cfl[ixy - 1], nthreads);
+        if (rc == ERR_NONPHYSICAL) bad = 1;
+        double *dst = (ixy == 1) ? qi : qout;
+        for (int j = 0; j < my; j++)
+            for (int i = 0; i < mx; i++)
+                for (int k = 0; k < m; k++)
+                    dst[(size_t)k + (size_t)m * ((size_t)i + (size_t)mx * j)] =
+                        qb[(size_t)k + (size_t)m * ((size_t)(i + g) + (size_t)nx * (j + g))];
+        src = qi;
+    }
+    free(qa); free(qb); free(qi);
+    *cfl_out = cfl[0] > cfl[1] ? cfl[0] : cfl[1];
+    if (rc && rc != ERR_NONPHYSICAL) return rc;
+    return bad ? ERR_NONPHYSICAL : 0;
 }

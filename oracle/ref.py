@@ -44,6 +44,13 @@ def lib():
         L.gclaw_ref_step2.argtypes = [ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       dp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_int, ctypes.c_int, ip, dp, ctypes.c_int]
+        L.gclaw_ref_step_split.argtypes = [ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, dp, dp,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_int, ip, ip, ip, dp, ctypes.c_int]
+        L.gclaw_ref_step2ds.argtypes = [ctypes.c_int, dp, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_int, ip, ctypes.c_int, dp,
+                                        ctypes.c_int]
         L.gclaw_ref_fill_ghosts.argtypes = [ctypes.c_int] * 4 + [ip, ip, dp, dp]
         L.gclaw_ref_rpn2.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp]
         L.gclaw_ref_rpt2.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, dp, dp, dp, dp]
@@ -112,6 +119,24 @@ def step(rp, pd, q, dx, dy, dt, bc_lower, bc_upper, order=2, tw=2, mthlim=(4, 4,
                               _ip(np.array(bc_upper, np.int32)), _dp(cfl), nthreads)
     if rc < 0:
         raise ValueError(f"gclaw_ref_step failed: {rc}")
+    return qout, float(cfl[0]), rc
+
+
+def step_split(rp, pd, q, dx, dy, dt, bc_lower, bc_upper, order=2, mthlim=(4, 4, 4, 4),
+               nthreads=1):
+    """PyClaw's dimensionally split step (x-sweep, boundary conditions, y-sweep)
+    on an interior (m, mx, my) array; returns (qnew, cfl, rc)."""
+    m, mx, my = q.shape
+    qf = np.asfortranarray(q, dtype=np.float64)
+    qout = np.zeros_like(qf, order="F")
+    cfl = np.zeros(1)
+    lim = np.zeros(4, np.int32)
+    lim[:len(mthlim)] = mthlim
+    rc = lib().gclaw_ref_step_split(rp, _dp(_pd(pd)), mx, my, _dp(qf), _dp(qout), dx, dy, dt,
+                                    order, _ip(lim), _ip(np.array(bc_lower, np.int32)),
+                                    _ip(np.array(bc_upper, np.int32)), _dp(cfl), nthreads)
+    if rc < 0:
+        raise ValueError(f"gclaw_ref_step_split failed: {rc}")
     return qout, float(cfl[0]), rc
 
 

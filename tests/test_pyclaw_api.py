@@ -46,10 +46,6 @@ def test_unsupported_options_fail_loudly():
     claw = workloads.make_claw(workloads.acoustics_radial(8, 8))
     s = claw.solver
     st = claw.solution.state
-    s.dimensional_split = True
-    with pytest.raises(NotImplementedError):
-        s.solver_struct(st)
-    s.dimensional_split = False
     s.kernel_language = "Fortran"
     with pytest.raises(NotImplementedError):
         s.solver_struct(st)
