@@ -42,13 +42,18 @@ def main(argv=None):
     p.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     p.add_argument("--adjoint", action="store_true")
     p.add_argument("--fp32-kernel", default="auto", choices=["auto", "tile", "strip"])
+    p.add_argument("--split", action="store_true", help="dimensionally split steps")
+    p.add_argument("--batched", type=int, default=0,
+                   help="time the first N problems of the seeded shallow-water ensemble")
     a = p.parse_args(argv)
     from . import _lib
 
     _lib.lib().gclaw_fp32_kernel({"auto": 0, "tile": 1, "strip": 2}[a.fp32_kernel])
+    if a.batched:
+        return run_batched(a)
     w = make_workload(a.workload, a.mx, a.my or a.mx)
     s = w.solver_struct(0 if a.precision == "fp64" else 1)
-    dev = DeviceProblem(s)
+    dev = DeviceProblem(s, split=a.split)
     dev.upload(w.q0)
     dev.ctrl_init(0.0, w.dt_initial, math.inf, cfl_max=w.cfl_max, cfl_desired=w.cfl_desired,
                   max_steps=10 ** 9)
@@ -64,10 +69,39 @@ def main(argv=None):
     ms = e0.elapsed_time(e1) / max(a.steps, 1)
     cells = w.mx * w.my
     print(json.dumps({"workload": w.name, "mx": w.mx, "my": w.my, "precision": a.precision,
-                      "steps": a.steps, "ms_per_step": ms,
+                      "split": a.split, "steps": a.steps, "ms_per_step": ms,
                       "gcell_updates_per_s": cells / (ms * 1e-3) * 1e-9 if ms > 0 else None,
                       "accepted": c.numsteps, "status": c.status, "cfl": c.cfl}))
     return 0 if c.status == 0 else 1
+
+
+def run_batched(a):
+    """--warmup then --steps batched launches over the first --batched
+    problems of the ensemble (FP32-bulk unless --precision fp64)."""
+    from . import _lib
+
+    e = workloads.batched_ensemble(nsteps=10 ** 6)
+    n = a.batched
+    e.shapes, e.deltas, e.params, e.dt0 = e.shapes[:n], e.deltas[:n], e.params[:n], e.dt0[:n]
+    prec = _lib.PREC_FP64 if a.precision == "fp64" else _lib.PREC_FP32_BULK
+    bs = workloads.make_batch(e, precision=prec)
+    bs.advance(a.warmup)
+    torch.cuda.synchronize()
+    c0 = bs.read_ctrls()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    bs.advance(a.steps)
+    e1.record()
+    torch.cuda.synchronize()
+    c1 = bs.read_ctrls()
+    ms = e0.elapsed_time(e1) / max(a.steps, 1)
+    upd = sum(int(mx) * int(my) * int(k1 - k0) for (mx, my), k0, k1 in
+              zip(e.shapes, c0["numsteps"], c1["numsteps"]))
+    print(json.dumps({"workload": f"ensemble[{n}]", "cells": e.cells, "precision": a.precision,
+                      "steps": a.steps, "ms_per_step": ms,
+                      "gcell_updates_per_s": upd / (ms * 1e-3 * max(a.steps, 1)) * 1e-9,
+                      "status_nonzero": int((c1["status"] != 0).sum())}))
+    return 0 if (c1["status"] == 0).all() else 1
 
 
 def run_adjoint(a, w, s, dev):

@@ -17,6 +17,7 @@
  *     riemann/src/rpn2_acoustics.f90,  rpt2_acoustics.f90
  *     riemann/src/rpn2_shallow_roe_with_efix.f90, rpt2_shallow_roe_with_efix.f90
  *     riemann/src/rpn2_euler_4wave.f90, rpt2_euler.f90
+ *     riemann/src/rpn2_vc_acoustics.f90, rpt2_vc_acoustics.f90
  * It is a restatement, in original code, of the published method that the
  * reference names as its algorithm source (CITATION.md:19-41):
  * R. J. LeVeque, J. Comput. Phys. 131 (1997) 327-353, and LeVeque, "Finite
@@ -46,6 +47,7 @@
 #define RP_ACOUSTICS 1
 #define RP_SHALLOW_ROE_EFIX 2
 #define RP_EULER_4WAVE 3
+#define RP_VC_ACOUSTICS 4
 
 #define BC_CUSTOM 0
 #define BC_EXTRAP 1
@@ -70,6 +72,7 @@ static int rp_shape(int id, int *m, int *mw)
     case RP_ACOUSTICS: *m = 3; *mw = 2; return 0;
     case RP_SHALLOW_ROE_EFIX: *m = 3; *mw = 3; return 0;
     case RP_EULER_4WAVE: *m = 4; *mw = 4; return 0;
+    case RP_VC_ACOUSTICS: *m = 3; *mw = 2; return 0;
     default: return ERR_ARG;
     }
 }
@@ -289,12 +292,42 @@ done:
     return bad;
 }
 
+/* Variable-coefficient acoustics, q = (p, u, v), aux = (rho, c) per cell:
+ * the interface Riemann problem between impedances Zl = rho_l c_l and
+ * Zr = rho_r c_r (FVMHP sec. 9.9; upstream rpn2_vc_acoustics.f90): speeds
+ * -c_l and +c_r, eigenvectors (-Zl, 1, 0) and (Zr, 1, 0).  With equal
+ * coefficients on both sides every expression equals rpn2_acoustics'. */
+static int rpn2_vc_acoustics(int ixy, const double *ql, const double *qr, const double *al,
+                             const double *ar, double *wave, double *s, double *amdq,
+                             double *apdq)
+{
+    const int mu = ixy, mv = 3 - ixy;
+    double d0 = qr[0] - ql[0];
+    double d1 = qr[mu] - ql[mu];
+    double zl = al[0] * al[1], zr = ar[0] * ar[1];
+    double a1 = (-d0 + zr * d1) / (zl + zr);
+    double a2 = (d0 + zl * d1) / (zl + zr);
+    double *w1 = wave, *w2 = wave + 3;
+    w1[0] = -a1 * zl; w1[mu] = a1; w1[mv] = 0.0;
+    s[0] = -al[1];
+    w2[0] = a2 * zr; w2[mu] = a2; w2[mv] = 0.0;
+    s[1] = ar[1];
+    for (int k = 0; k < 3; k++) {
+        amdq[k] = s[0] * w1[k];
+        apdq[k] = s[1] * w2[k];
+    }
+    return 0;
+}
+
+/* al / ar: aux of the cells left / right of the edge (solvers with aux). */
 static int rpn2(const rp_t *rp, int ixy, const double *ql, const double *qr,
-                double *wave, double *s, double *amdq, double *apdq)
+                const double *al, const double *ar, double *wave, double *s, double *amdq,
+                double *apdq)
 {
     switch (rp->id) {
     case RP_ACOUSTICS: return rpn2_acoustics(rp, ixy, ql, qr, wave, s, amdq, apdq);
     case RP_SHALLOW_ROE_EFIX: return rpn2_shallow(rp, ixy, ql, qr, wave, s, amdq, apdq);
+    case RP_VC_ACOUSTICS: return rpn2_vc_acoustics(ixy, ql, qr, al, ar, wave, s, amdq, apdq);
     default: return rpn2_euler(rp, ixy, ql, qr, wave, s, amdq, apdq);
     }
 }
@@ -388,12 +421,35 @@ static void rpt2_euler(const rp_t *rp, int ixy, const double *ql, const double *
     split_sum(4, 4, sb, wb, bm, bp);
 }
 
+/* Variable-coefficient acoustics: the fluctuation asdq entering a cell is
+ * split into the part transmitted down into the cell below (speed -c_m,
+ * eigenvector (-Zm, 0, 1) against the cell's own impedance Z) and the part
+ * transmitted up into the cell above (speed +c_p, eigenvector (Zp, 0, 1));
+ * reflection at the interfaces is what the two parts do not carry
+ * (upstream rpt2_vc_acoustics.f90).  am / a0 / ap: aux of the cells below,
+ * at and above the cell that receives asdq. */
+static void rpt2_vc_acoustics(int ixy, const double *am, const double *a0, const double *ap,
+                              const double *asdq, double *bm, double *bp)
+{
+    const int mu = ixy, mv = 3 - ixy;
+    const double cm = am[1], cp = ap[1];
+    const double zm = am[0] * am[1], zz = a0[0] * a0[1], zp = ap[0] * ap[1];
+    double a1 = (-asdq[0] + zz * asdq[mv]) / (zm + zz);
+    double a2 = (asdq[0] + zz * asdq[mv]) / (zz + zp);
+    bm[0] = cm * a1 * zm; bm[mu] = 0.0; bm[mv] = -cm * a1;
+    bp[0] = cp * a2 * zp; bp[mu] = 0.0; bp[mv] = cp * a2;
+}
+
+/* am / a0 / ap: aux of the cells below / at / above the cell that receives
+ * asdq (cell e-1 for amdq, cell e for apdq), for solvers with aux. */
 static void rpt2(const rp_t *rp, int ixy, const double *ql, const double *qr,
+                 const double *am, const double *a0, const double *ap,
                  const double *asdq, double *bm, double *bp)
 {
     switch (rp->id) {
     case RP_ACOUSTICS: rpt2_acoustics(rp, ixy, ql, qr, asdq, bm, bp); return;
     case RP_SHALLOW_ROE_EFIX: rpt2_shallow(rp, ixy, ql, qr, asdq, bm, bp); return;
+    case RP_VC_ACOUSTICS: rpt2_vc_acoustics(ixy, am, a0, ap, asdq, bm, bp); return;
     default: rpt2_euler(rp, ixy, ql, qr, asdq, bm, bp); return;
     }
 }
@@ -432,7 +488,8 @@ typedef struct {
 static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double dtdx,
                        int order, int tw, const int *mthlim,
                        double *qadd, double *fadd, double *g1, double *g2, double *cfl1d,
-                       const work_t *wk)
+                       const work_t *wk, int maux, const double *auxm, const double *aux0,
+                       const double *auxp)
 {
     const int m = rp->m, mw = rp->mw;
     const int off = 2;
@@ -446,9 +503,11 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
 #define BM(e) (wk->bm + (size_t)((e) + off) * m)
 #define BP(e) (wk->bp + (size_t)((e) + off) * m)
 #define A1(arr, c) ((arr) + (size_t)((c) + off) * m)
+#define AX(arr, c) ((arr) ? (arr) + (size_t)((c) + off) * maux : NULL)
 
     for (e = -1; e <= n + 1; e++)
-        bad |= rpn2(rp, ixy, Q(e - 1), Q(e), W(e), S(e), AM(e), AP(e));
+        bad |= rpn2(rp, ixy, Q(e - 1), Q(e), AX(aux0, e - 1), AX(aux0, e), W(e), S(e), AM(e),
+                    AP(e));
 
     for (e = -2; e <= n + 1; e++)
         for (k = 0; k < m; k++) {
@@ -516,13 +575,17 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
                     AP(e)[k] = AP(e)[k] - CQ(e)[k];
                 }
         const double h = 0.5 * dtdx;
-        for (e = 0; e <= n; e++) rpt2(rp, ixy, Q(e - 1), Q(e), AM(e), BM(e), BP(e));
+        for (e = 0; e <= n; e++)
+            rpt2(rp, ixy, Q(e - 1), Q(e), AX(auxm, e - 1), AX(aux0, e - 1), AX(auxp, e - 1),
+                 AM(e), BM(e), BP(e));
         for (e = 0; e <= n; e++)
             for (k = 0; k < m; k++) {
                 A1(g1, e - 1)[k] = A1(g1, e - 1)[k] - h * BM(e)[k];
                 A1(g2, e - 1)[k] = A1(g2, e - 1)[k] - h * BP(e)[k];
             }
-        for (e = 0; e <= n; e++) rpt2(rp, ixy, Q(e - 1), Q(e), AP(e), BM(e), BP(e));
+        for (e = 0; e <= n; e++)
+            rpt2(rp, ixy, Q(e - 1), Q(e), AX(auxm, e), AX(aux0, e), AX(auxp, e), AP(e), BM(e),
+                 BP(e));
         for (e = 0; e <= n; e++)
             for (k = 0; k < m; k++) {
                 A1(g1, e)[k] = A1(g1, e)[k] - h * BM(e)[k];
@@ -538,6 +601,7 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
 #undef BM
 #undef BP
 #undef A1
+#undef AX
     return bad;
 }
 
@@ -553,8 +617,25 @@ int gclaw_ref_shape(int rp_id, int *m, int *mw) { return rp_shape(rp_id, m, mw);
  * edge cell, periodic wraps, wall mirrors and negates the normal
  * momentum/velocity component (component 1 for x, 2 for y).  q is (m,mx,my)
  * Fortran order, qbc is (m,mx+2g,my+2g). */
+static int fill_ghosts_impl(int m, int mx, int my, int g, const int *bc_lower,
+                            const int *bc_upper, const double *q, double *qbc, int negate);
+
 int gclaw_ref_fill_ghosts(int m, int mx, int my, int g, const int *bc_lower,
                           const int *bc_upper, const double *q, double *qbc)
+{
+    return fill_ghosts_impl(m, mx, my, g, bc_lower, bc_upper, q, qbc, 1);
+}
+
+/* Ghost fill of an aux array (PyClaw's aux_bc_lower / aux_bc_upper): as for
+ * q, except that wall boundaries mirror without negating any component. */
+int gclaw_ref_fill_aux_ghosts(int maux, int mx, int my, int g, const int *bc_lower,
+                              const int *bc_upper, const double *aux, double *auxbc)
+{
+    return fill_ghosts_impl(maux, mx, my, g, bc_lower, bc_upper, aux, auxbc, 0);
+}
+
+static int fill_ghosts_impl(int m, int mx, int my, int g, const int *bc_lower,
+                            const int *bc_upper, const double *q, double *qbc, int negate)
 {
     if (m < 1 || m > MAXM || mx < g || my < g || g < 1) return ERR_ARG;
     for (int d = 0; d < 2; d++)
@@ -574,12 +655,12 @@ int gclaw_ref_fill_ghosts(int m, int mx, int my, int g, const int *bc_lower,
             switch (bc_lower[0]) {
             case BC_EXTRAP: src_lo = g; break;
             case BC_PERIODIC: src_lo = l + mx; break;
-            default: src_lo = 2 * g - 1 - l; neg_lo = 1; break;
+            default: src_lo = 2 * g - 1 - l; neg_lo = negate; break;
             }
             switch (bc_upper[0]) {
             case BC_EXTRAP: src_hi = g + mx - 1; break;
             case BC_PERIODIC: src_hi = g + l; break;
-            default: src_hi = g + mx - 1 - l; neg_hi = 1; break;
+            default: src_hi = g + mx - 1 - l; neg_hi = negate; break;
             }
             for (int k = 0; k < m; k++) {
                 double vlo = QB(k, src_lo, j), vhi = QB(k, src_hi, j);
@@ -594,12 +675,12 @@ int gclaw_ref_fill_ghosts(int m, int mx, int my, int g, const int *bc_lower,
             switch (bc_lower[1]) {
             case BC_EXTRAP: src_lo = g; break;
             case BC_PERIODIC: src_lo = l + my; break;
-            default: src_lo = 2 * g - 1 - l; neg_lo = 1; break;
+            default: src_lo = 2 * g - 1 - l; neg_lo = negate; break;
             }
             switch (bc_upper[1]) {
             case BC_EXTRAP: src_hi = g + my - 1; break;
             case BC_PERIODIC: src_hi = g + l; break;
-            default: src_hi = g + my - 1 - l; neg_hi = 1; break;
+            default: src_hi = g + my - 1 - l; neg_hi = negate; break;
             }
             for (int k = 0; k < m; k++) {
                 double vlo = QB(k, i, src_lo), vhi = QB(k, i, src_hi);
@@ -618,8 +699,21 @@ int gclaw_ref_rpn2(int rp_id, const double *pd, int ixy, const double *ql, const
     rp_t rp;
     rp.id = rp_id;
     if (rp_shape(rp_id, &rp.m, &rp.mw) || (ixy != 1 && ixy != 2)) return ERR_ARG;
+    if (rp_id == RP_VC_ACOUSTICS) return ERR_ARG; /* needs aux: gclaw_ref_rpn2_aux */
     memcpy(rp.pd, pd, sizeof rp.pd);
-    return rpn2(&rp, ixy, ql, qr, wave, s, amdq, apdq) ? ERR_NONPHYSICAL : 0;
+    return rpn2(&rp, ixy, ql, qr, NULL, NULL, wave, s, amdq, apdq) ? ERR_NONPHYSICAL : 0;
+}
+
+/* The same with the aux values of the two cells (solvers with aux). */
+int gclaw_ref_rpn2_aux(int rp_id, const double *pd, int ixy, const double *ql,
+                       const double *qr, const double *al, const double *ar, double *wave,
+                       double *s, double *amdq, double *apdq)
+{
+    rp_t rp;
+    rp.id = rp_id;
+    if (rp_shape(rp_id, &rp.m, &rp.mw) || (ixy != 1 && ixy != 2)) return ERR_ARG;
+    memcpy(rp.pd, pd, sizeof rp.pd);
+    return rpn2(&rp, ixy, ql, qr, al, ar, wave, s, amdq, apdq) ? ERR_NONPHYSICAL : 0;
 }
 
 int gclaw_ref_rpt2(int rp_id, const double *pd, int ixy, const double *ql, const double *qr,
@@ -628,8 +722,22 @@ int gclaw_ref_rpt2(int rp_id, const double *pd, int ixy, const double *ql, const
     rp_t rp;
     rp.id = rp_id;
     if (rp_shape(rp_id, &rp.m, &rp.mw) || (ixy != 1 && ixy != 2)) return ERR_ARG;
+    if (rp_id == RP_VC_ACOUSTICS) return ERR_ARG; /* needs aux: gclaw_ref_rpt2_aux */
     memcpy(rp.pd, pd, sizeof rp.pd);
-    rpt2(&rp, ixy, ql, qr, asdq, bm, bp);
+    rpt2(&rp, ixy, ql, qr, NULL, NULL, NULL, asdq, bm, bp);
+    return 0;
+}
+
+/* The same with the aux of the cells below, at and above the receiving cell. */
+int gclaw_ref_rpt2_aux(int rp_id, const double *pd, int ixy, const double *am,
+                       const double *a0, const double *ap, const double *asdq, double *bm,
+                       double *bp)
+{
+    rp_t rp;
+    rp.id = rp_id;
+    if (rp_shape(rp_id, &rp.m, &rp.mw) || (ixy != 1 && ixy != 2)) return ERR_ARG;
+    memcpy(rp.pd, pd, sizeof rp.pd);
+    rpt2(&rp, ixy, NULL, NULL, am, a0, ap, asdq, bm, bp);
     return 0;
 }
 
@@ -644,14 +752,27 @@ double gclaw_ref_philim(int id, double r) { return philim(id, r); }
 static int step2_dirs(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
                       double *qnew, double dx, double dy, double dt, int order, int tw,
                       const int *mthlim, double *cfl_out, int nthreads, int ixy_lo,
-                      int ixy_hi);
+                      int ixy_hi, int maux, const double *auxbc);
 
 int gclaw_ref_step2(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
                     double *qnew, double dx, double dy, double dt, int order, int tw,
                     const int *mthlim, double *cfl_out, int nthreads)
 {
+    if (rp_id == RP_VC_ACOUSTICS) return ERR_ARG; /* needs aux: gclaw_ref_step2_aux */
     return step2_dirs(rp_id, pd, g, mx, my, qold, qnew, dx, dy, dt, order, tw, mthlim, cfl_out,
-                      nthreads, 1, 2);
+                      nthreads, 1, 2, 0, NULL);
+}
+
+/* step2 for solvers with an aux array: auxbc is (maux, mx+2g, my+2g),
+ * Fortran order, ghosts filled (gclaw_ref_fill_aux_ghosts). */
+int gclaw_ref_step2_aux(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
+                        double *qnew, int maux, const double *auxbc, double dx, double dy,
+                        double dt, int order, int tw, const int *mthlim, double *cfl_out,
+                        int nthreads)
+{
+    if (maux < 1 || maux > MAXM || !auxbc) return ERR_ARG;
+    return step2_dirs(rp_id, pd, g, mx, my, qold, qnew, dx, dy, dt, order, tw, mthlim, cfl_out,
+                      nthreads, 1, 2, maux, auxbc);
 }
 
 /* One sweep of PyClaw's dimensionally split step (classic2 step2ds,
@@ -663,13 +784,15 @@ int gclaw_ref_step2ds(int rp_id, const double *pd, int g, int mx, int my, const 
                       const int *mthlim, int ixy, double *cfl_out, int nthreads)
 {
     if (ixy != 1 && ixy != 2) return ERR_ARG;
+    if (rp_id == RP_VC_ACOUSTICS) return ERR_ARG;
     return step2_dirs(rp_id, pd, g, mx, my, qold, qnew, dx, dy, dt, order, 0, mthlim, cfl_out,
-                      nthreads, ixy, ixy);
+                      nthreads, ixy, ixy, 0, NULL);
 }
 
 static int step2_dirs(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
                       double *qnew, double dx, double dy, double dt, int order, int tw,
-                      const int *mthlim, double *cfl_out, int nthreads, int ixy_lo, int ixy_hi)
+                      const int *mthlim, double *cfl_out, int nthreads, int ixy_lo, int ixy_hi,
+                      int maux, const double *auxbc)
 {
     rp_t rp;
     rp.id = rp_id;
@@ -715,6 +838,10 @@ static int step2_dirs(int rp_id, const double *pd, int g, int mx, int my, const 
             wk.cqxx = malloc(sizeof(double) * per);
             wk.bm = malloc(sizeof(double) * per);
             wk.bp = malloc(sizeof(double) * per);
+            /* aux of the slice and of the slices below and above it */
+            double *a1d[3] = {NULL, NULL, NULL};
+            if (maux)
+                for (int d = 0; d < 3; d++) a1d[d] = malloc(sizeof(double) * (size_t)nmax * maux);
 #pragma omp for schedule(static)
             for (int sl = 0; sl < ns; sl++) {
                 /* slice index sl -> row j = sl-1 (x-sweep) or column i = sl-1 */
@@ -725,9 +852,21 @@ static int step2_dirs(int rp_id, const double *pd, int g, int mx, int my, const 
                                          : (size_t)k + (size_t)m * ((size_t)(sl - 1 + g) + (size_t)nx * (c + g));
                         q1d[(size_t)(c + 2) * m + k] = qold[src];
                     }
+                for (int d = 0; d < 3 && maux; d++) {
+                    const int t = sl - 2 + d; /* transverse index of slice sl-1+d-1 */
+                    for (int c = -2; c < n + 2; c++)
+                        for (int k = 0; k < maux; k++) {
+                            size_t src = (ixy == 1)
+                                             ? (size_t)k + (size_t)maux * ((size_t)(c + g) + (size_t)nx * (t + g))
+                                             : (size_t)k + (size_t)maux * ((size_t)(t + g) + (size_t)nx * (c + g));
+                            a1d[d][(size_t)(c + 2) * maux + k] = auxbc[src];
+                        }
+                }
                 bad |= flux2_slice(&rp, ixy, n, q1d, dtdn, order, tw, mthlim, QA + per * sl,
-                                   FA + per * sl, G1 + per * sl, G2 + per * sl, &cfls[sl], &wk);
+                                   FA + per * sl, G1 + per * sl, G2 + per * sl, &cfls[sl], &wk,
+                                   maux, a1d[0], a1d[1], a1d[2]);
             }
+            for (int d = 0; d < 3; d++) free(a1d[d]);
             free(q1d); free(wk.wave); free(wk.s); free(wk.amdq); free(wk.apdq);
             free(wk.cqxx); free(wk.bm); free(wk.bp);
         }
@@ -835,4 +974,37 @@ int gclaw_ref_step_split(int rp_id, const double *pd, int mx, int my, const doub
     *cfl_out = cfl[0] > cfl[1] ? cfl[0] : cfl[1];
     if (rc && rc != ERR_NONPHYSICAL) return rc;
     return bad ? ERR_NONPHYSICAL : 0;
+}
+
+/* Ghost fill of q and aux + step2 on interior-shaped arrays, for solvers
+ * with an aux array (m, mx, my) / (maux, mx, my). */
+int gclaw_ref_step_aux(int rp_id, const double *pd, int mx, int my, const double *q,
+                       double *qout, int maux, const double *aux, double dx, double dy,
+                       double dt, int order, int tw, const int *mthlim, const int *bc_lower,
+                       const int *bc_upper, const int *aux_bc_lower, const int *aux_bc_upper,
+                       double *cfl_out, int nthreads)
+{
+    int m, mw;
+    if (rp_shape(rp_id, &m, &mw) || maux < 1 || maux > MAXM) return ERR_ARG;
+    const int g = 2, nx = mx + 4, ny = my + 4;
+    size_t nb = (size_t)m * nx * ny;
+    double *qa = malloc(sizeof(double) * nb), *qb = malloc(sizeof(double) * nb);
+    double *ab = malloc(sizeof(double) * (size_t)maux * nx * ny);
+    if (!qa || !qb || !ab) {
+        free(qa); free(qb); free(ab);
+        return ERR_ALLOC;
+    }
+    int rc = gclaw_ref_fill_ghosts(m, mx, my, g, bc_lower, bc_upper, q, qa);
+    if (rc == 0) rc = gclaw_ref_fill_aux_ghosts(maux, mx, my, g, aux_bc_lower, aux_bc_upper, aux, ab);
+    if (rc == 0)
+        rc = gclaw_ref_step2_aux(rp_id, pd, g, mx, my, qa, qb, maux, ab, dx, dy, dt, order, tw,
+                                 mthlim, cfl_out, nthreads);
+    if (rc == 0 || rc == ERR_NONPHYSICAL)
+        for (int j = 0; j < my; j++)
+            for (int i = 0; i < mx; i++)
+                for (int k = 0; k < m; k++)
+                    qout[(size_t)k + (size_t)m * ((size_t)i + (size_t)mx * j)] =
+                        qb[(size_t)k + (size_t)m * ((size_t)(i + g) + (size_t)nx * (j + g))];
+    free(qa); free(qb); free(ab);
+    return rc;
 }

@@ -20,8 +20,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libclassic2_ref.so")
 
-RP_ACOUSTICS, RP_SHALLOW, RP_EULER = 1, 2, 3
-SHAPES = {RP_ACOUSTICS: (3, 2), RP_SHALLOW: (3, 3), RP_EULER: (4, 4)}
+RP_ACOUSTICS, RP_SHALLOW, RP_EULER, RP_VC_ACOUSTICS = 1, 2, 3, 4
+SHAPES = {RP_ACOUSTICS: (3, 2), RP_SHALLOW: (3, 3), RP_EULER: (4, 4), RP_VC_ACOUSTICS: (3, 2)}
 
 _lib = None
 
@@ -52,6 +52,18 @@ def lib():
                                         ctypes.c_double, ctypes.c_int, ip, ctypes.c_int, dp,
                                         ctypes.c_int]
         L.gclaw_ref_fill_ghosts.argtypes = [ctypes.c_int] * 4 + [ip, ip, dp, dp]
+        L.gclaw_ref_fill_aux_ghosts.argtypes = [ctypes.c_int] * 4 + [ip, ip, dp, dp]
+        L.gclaw_ref_step_aux.argtypes = [ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, dp, dp,
+                                         ctypes.c_int, dp, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_int, ctypes.c_int, ip, ip, ip,
+                                         ip, ip, dp, ctypes.c_int]
+        L.gclaw_ref_step2_aux.argtypes = [ctypes.c_int, dp, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, dp, dp, ctypes.c_int, dp, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                          ctypes.c_int, ip, dp, ctypes.c_int]
+        L.gclaw_ref_rpn2_aux.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp,
+                                         dp, dp]
+        L.gclaw_ref_rpt2_aux.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp]
         L.gclaw_ref_rpn2.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp]
         L.gclaw_ref_rpt2.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, dp, dp, dp, dp]
         L.gclaw_ref_philim.argtypes = [ctypes.c_int, ctypes.c_double]
@@ -120,6 +132,56 @@ def step(rp, pd, q, dx, dy, dt, bc_lower, bc_upper, order=2, tw=2, mthlim=(4, 4,
     if rc < 0:
         raise ValueError(f"gclaw_ref_step failed: {rc}")
     return qout, float(cfl[0]), rc
+
+
+def step_aux(rp, pd, q, aux, dx, dy, dt, bc_lower, bc_upper, aux_bc_lower, aux_bc_upper,
+             order=2, tw=2, mthlim=(4, 4, 4, 4), nthreads=1):
+    """Ghost fill of q and aux + step for solvers with an aux array (maux, mx,
+    my); returns (qnew, cfl, rc)."""
+    m, mx, my = q.shape
+    qf = np.asfortranarray(q, dtype=np.float64)
+    af = np.asfortranarray(aux, dtype=np.float64)
+    qout = np.zeros_like(qf, order="F")
+    cfl = np.zeros(1)
+    lim = np.zeros(4, np.int32)
+    lim[:len(mthlim)] = mthlim
+    i32 = lambda v: _ip(np.array(v, np.int32))  # noqa: E731
+    rc = lib().gclaw_ref_step_aux(rp, _dp(_pd(pd)), mx, my, _dp(qf), _dp(qout), af.shape[0],
+                                  _dp(af), dx, dy, dt, order, tw, _ip(lim), i32(bc_lower),
+                                  i32(bc_upper), i32(aux_bc_lower), i32(aux_bc_upper), _dp(cfl),
+                                  nthreads)
+    if rc < 0:
+        raise ValueError(f"gclaw_ref_step_aux failed: {rc}")
+    return qout, float(cfl[0]), rc
+
+
+def fill_aux_ghosts(aux, bc_lower, bc_upper):
+    maux, mx, my = aux.shape
+    af = np.asfortranarray(aux, dtype=np.float64)
+    abc = np.zeros((maux, mx + 4, my + 4), order="F")
+    rc = lib().gclaw_ref_fill_aux_ghosts(maux, mx, my, 2, _ip(np.array(bc_lower, np.int32)),
+                                         _ip(np.array(bc_upper, np.int32)), _dp(af), _dp(abc))
+    if rc:
+        raise ValueError(f"gclaw_ref_fill_aux_ghosts failed: {rc}")
+    return abc
+
+
+def rpn2_aux(rp, pd, ixy, ql, qr, al, ar):
+    m, mw = SHAPES[rp]
+    wave, s, amdq, apdq = np.zeros(mw * m), np.zeros(mw), np.zeros(m), np.zeros(m)
+    f = lambda a: _dp(np.ascontiguousarray(a, float))  # noqa: E731
+    rc = lib().gclaw_ref_rpn2_aux(rp, _dp(_pd(pd)), ixy, f(ql), f(qr), f(al), f(ar), _dp(wave),
+                                  _dp(s), _dp(amdq), _dp(apdq))
+    return wave.reshape(mw, m), s, amdq, apdq, rc
+
+
+def rpt2_aux(rp, pd, ixy, am, a0, ap, asdq):
+    m = SHAPES[rp][0]
+    bm, bp = np.zeros(m), np.zeros(m)
+    f = lambda a: _dp(np.ascontiguousarray(a, float))  # noqa: E731
+    lib().gclaw_ref_rpt2_aux(rp, _dp(_pd(pd)), ixy, f(am), f(a0), f(ap), f(asdq), _dp(bm),
+                             _dp(bp))
+    return bm, bp
 
 
 def step_split(rp, pd, q, dx, dy, dt, bc_lower, bc_upper, order=2, mthlim=(4, 4, 4, 4),

@@ -1,15 +1,16 @@
 """Shared builders for the tests: random physical states per solver."""
 import numpy as np
 
-RP_ACOUSTICS, RP_SHALLOW, RP_EULER = 1, 2, 3
-SHAPES = {RP_ACOUSTICS: (3, 2), RP_SHALLOW: (3, 3), RP_EULER: (4, 4)}
-PD = {RP_ACOUSTICS: [1.0, 4.0, 2.0, 2.0], RP_SHALLOW: [1.0], RP_EULER: [1.4, 1.0]}
+RP_ACOUSTICS, RP_SHALLOW, RP_EULER, RP_VC_ACOUSTICS = 1, 2, 3, 4
+SHAPES = {RP_ACOUSTICS: (3, 2), RP_SHALLOW: (3, 3), RP_EULER: (4, 4), RP_VC_ACOUSTICS: (3, 2)}
+PD = {RP_ACOUSTICS: [1.0, 4.0, 2.0, 2.0], RP_SHALLOW: [1.0], RP_EULER: [1.4, 1.0],
+      RP_VC_ACOUSTICS: []}
 
 
 def random_state(rp, mx, my, rng):
     m = SHAPES[rp][0]
     q = np.empty((m, mx, my), order="F")
-    if rp == RP_ACOUSTICS:
+    if rp in (RP_ACOUSTICS, RP_VC_ACOUSTICS):
         q[:] = rng.normal(size=(m, mx, my))
     elif rp == RP_SHALLOW:
         q[0] = 1.0 + rng.random((mx, my))
@@ -29,3 +30,13 @@ def random_state(rp, mx, my, rng):
 
 def rel_l1(a, b):
     return float(np.abs(a - b).sum() / np.abs(b).sum())
+
+
+def random_medium(mx, my, rng):
+    """aux = (rho, c) of a layered, noisy medium for variable-coefficient
+    acoustics: densities in [0.5, 3], sound speeds in [0.5, 2.5]."""
+    aux = np.empty((2, mx, my), order="F")
+    layer = (np.arange(mx)[:, None] + 2 * np.arange(my)[None, :]) % 7 < 3
+    aux[0] = np.where(layer, 2.5, 0.6) + 0.4 * rng.random((mx, my))
+    aux[1] = np.where(layer, 0.6, 2.0) + 0.4 * rng.random((mx, my))
+    return aux
