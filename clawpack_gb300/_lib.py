@@ -20,6 +20,7 @@ STRICT_LIB_PATH = os.path.join(HERE, "libgclaw_strict.so")
 RP_ACOUSTICS_2D = 1
 RP_SHALLOW_ROE_WITH_EFIX_2D = 2
 RP_EULER_4WAVE_2D = 3
+RP_VC_ACOUSTICS_2D = 4
 
 PREC_FP64 = 0
 PREC_FP32_BULK = 1
@@ -52,6 +53,9 @@ class GclawSolver(ctypes.Structure):
         ("transverse_waves", ctypes.c_int),
         ("precision", ctypes.c_int),
         ("problem_data", ctypes.c_double * 8),
+        ("aux", ctypes.c_void_p),
+        ("aux_bc_lower", ctypes.c_int * 2),
+        ("aux_bc_upper", ctypes.c_int * 2),
     ]
 
 

@@ -263,6 +263,7 @@ int gclaw_batch_advance(const gclaw_solver *s, const void *table_dev, int nprob,
          : launch_batch<RPT, float>(s, a, table_dev, nprob, total_tiles, q0_dev, q1_dev,        \
                                     ctrls_dev, nlaunch, st))
     switch (s->rp) {
+    case GCLAW_RP_VC_ACOUSTICS_2D: return GCLAW_ERR_UNSUPPORTED;  // no per-problem aux
     case GCLAW_RP_ACOUSTICS_2D: return GCLAW_BATCH(RpAcoustics);
     case GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D: return GCLAW_BATCH(RpShallow);
     default: return GCLAW_BATCH(RpEuler);

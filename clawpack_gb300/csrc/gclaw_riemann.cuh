@@ -149,7 +149,8 @@ __device__ __forceinline__ bool no_right_sonic_point(T h, T m, T g) {
 // ---------------------------------------------------------------------------
 template <typename T>
 struct RpAcoustics {
-    static constexpr int M = 3, MW = 2, NR = 0, NA = 0;
+    static constexpr int M = 3, MW = 2, NR = 0, NA = 0, NUA = 0;
+    static constexpr bool TNB = false;  // rpn2 does not read the transverse neighbours
     struct Params {
         T cc, zz;
     };
@@ -193,6 +194,76 @@ struct RpAcoustics {
     }
 };
 
+// ---------------------------------------------------------------------------
+// Variable-coefficient acoustics (upstream riemann/src/rpn2_vc_acoustics.f90,
+// rpt2_vc_acoustics.f90): q = (p, u, v), a user aux array (rho, c) per cell,
+// loaded into the per-cell aux area and turned into (Z = rho c, c) there.
+// rpn2 solves the interface problem between impedances Zl and Zr (speeds
+// -c_l, +c_r); rpt2 transmits a fluctuation into the cells below and above
+// the receiving cell with their speeds and impedances, so rpn2 also reads
+// the aux of the cells below and above both edge cells (TNB) and keeps them
+// in the edge record R = (c_m, Z_m, Z, c_p, Z_p) of the left cell, then of
+// the right cell.  With equal coefficients every expression equals
+// RpAcoustics' (bit for bit with -fmad=false).
+// ---------------------------------------------------------------------------
+template <typename T>
+struct RpVcAcoustics {
+    static constexpr int M = 3, MW = 2, NR = 10, NA = 2, NUA = 2;
+    static constexpr bool TNB = true;
+    struct Params {
+        int unused;
+    };
+    static Params make(const double *) { return Params{0}; }
+
+    template <int IXY>
+    __host__ __device__ static constexpr bool wnz(int p, int k) { return k != 3 - IXY; }
+
+    // aux holds the cell's (rho, c) on entry and (Z, c) on return
+    __device__ __forceinline__ static void cell_aux_user(const Params &, const T *, T *aux) {
+        aux[0] = aux[0] * aux[1];
+    }
+
+    // al / ar: (Z, c) of the edge cells; bl, tl / br, tr: of the cells below
+    // and above the left / right cell in the transverse direction
+    template <int IXY>
+    __device__ __forceinline__ static bool rpn2_nb(const Params &, const T *ql, const T *qr,
+                                                   const T *al, const T *ar, const T *bl,
+                                                   const T *tl, const T *br, const T *tr, T *W,
+                                                   T *s, T *am, T *ap, T *R) {
+        constexpr int mu = IXY, mv = 3 - IXY;
+        const T d0 = qr[0] - ql[0];
+        const T d1 = qr[mu] - ql[mu];
+        const T zl = al[0], zr = ar[0];
+        const T a1 = (-d0 + zr * d1) / (zl + zr);
+        const T a2 = (d0 + zl * d1) / (zl + zr);
+        W[0] = -a1 * zl; W[mu] = a1; W[mv] = (T)0;
+        s[0] = -al[1];
+        W[3] = a2 * zr; W[3 + mu] = a2; W[3 + mv] = (T)0;
+        s[1] = ar[1];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            am[k] = s[0] * W[k];
+            ap[k] = s[1] * W[3 + k];
+        }
+        R[0] = bl[1]; R[1] = bl[0]; R[2] = zl; R[3] = tl[1]; R[4] = tl[0];
+        R[5] = br[1]; R[6] = br[0]; R[7] = zr; R[8] = tr[1]; R[9] = tr[0];
+        return false;
+    }
+
+    // SIDE 0: asdq = amdq into the left cell; SIDE 1: apdq into the right cell
+    template <int IXY, int SIDE>
+    __device__ __forceinline__ static void rpt2s(const Params &, const T *R, const T *asdq, T *bm,
+                                                 T *bp) {
+        constexpr int mu = IXY, mv = 3 - IXY;
+        const T *r = R + 5 * SIDE;
+        const T cm = r[0], zm = r[1], zz = r[2], cp = r[3], zp = r[4];
+        const T a1 = (-asdq[0] + zz * asdq[mv]) / (zm + zz);
+        const T a2 = (asdq[0] + zz * asdq[mv]) / (zz + zp);
+        bm[0] = cm * a1 * zm; bm[mu] = (T)0; bm[mv] = -cm * a1;
+        bp[0] = cp * a2 * zp; bp[mu] = (T)0; bp[mv] = cp * a2;
+    }
+};
+
 // Sum of min(sb,0) Wb and max(sb,0) Wb over the transverse waves.
 template <typename T, int M, int MW>
 __device__ __forceinline__ void split_sum(const T *sb, const T *wb, T *bm, T *bp) {
@@ -215,7 +286,8 @@ __device__ __forceinline__ void split_sum(const T *sb, const T *wb, T *bm, T *bp
 // ---------------------------------------------------------------------------
 template <typename T>
 struct RpShallow {
-    static constexpr int M = 3, MW = 3, NR = 4, NA = 6;
+    static constexpr int M = 3, MW = 3, NR = 4, NA = 6, NUA = 0;
+    static constexpr bool TNB = false;
     struct Params {
         T g;
         double gd;
@@ -404,7 +476,8 @@ struct RpShallow {
 // ---------------------------------------------------------------------------
 template <typename T>
 struct RpEuler {
-    static constexpr int M = 4, MW = 4, NR = 7, NA = 8;
+    static constexpr int M = 4, MW = 4, NR = 7, NA = 8, NUA = 0;
+    static constexpr bool TNB = false;
     struct Params {
         T gamma, gamma1;
         int efix;

@@ -24,6 +24,8 @@ struct StepArgs {
     int bc_lo[2], bc_hi[2];
     int mthlim;  // limiter id of wave p in bits 8p..8p+7
     int order, tw;
+    const double *aux;           // per-cell aux (solvers with NUA > 0), laid out like q
+    int abc_lo[2], abc_hi[2];    // its boundary conditions (walls mirror, no negation)
     int sweeps;     // 1: x-sweep only, 2: y-sweep only (dimensional splitting); else both
     int no_finish;  // last block resets the block counter but leaves the CFL
                     // reduction to the next launch (first sweep of a split step)
@@ -66,6 +68,33 @@ __device__ __forceinline__ double load_q(const StepArgs &a, const double *__rest
     }
     double v = __ldg(q + k + (size_t)M * ((size_t)si + (size_t)a.mx * (size_t)sj));
     return neg ? -v : v;
+}
+
+// Component k of the ghost-filled aux array at (gi, gj), as load_q maps q but
+// with the aux boundary conditions (a wall mirrors without negation).
+template <int NUA>
+__device__ __forceinline__ double load_a(const StepArgs &a, int k, int gi, int gj) {
+    gi = min(max(gi, -2), a.mx + 1);
+    gj = min(max(gj, -2), a.my + 1);
+    if (a.ghosted)
+        return __ldg(a.aux + k +
+                     (size_t)NUA * ((size_t)(gi + 2) + (size_t)(a.mx + 4) * (size_t)(gj + 2)));
+    int sj = gj, si = gi;
+    if (gj < 0) {
+        const int b = a.abc_lo[1];
+        sj = b == GCLAW_BC_EXTRAP ? 0 : (b == GCLAW_BC_PERIODIC ? gj + a.my : -1 - gj);
+    } else if (gj >= a.my) {
+        const int b = a.abc_hi[1];
+        sj = b == GCLAW_BC_EXTRAP ? a.my - 1 : (b == GCLAW_BC_PERIODIC ? gj - a.my : 2 * a.my - 1 - gj);
+    }
+    if (gi < 0) {
+        const int b = a.abc_lo[0];
+        si = b == GCLAW_BC_EXTRAP ? 0 : (b == GCLAW_BC_PERIODIC ? gi + a.mx : -1 - gi);
+    } else if (gi >= a.mx) {
+        const int b = a.abc_hi[0];
+        si = b == GCLAW_BC_EXTRAP ? a.mx - 1 : (b == GCLAW_BC_PERIODIC ? gi - a.mx : 2 * a.mx - 1 - gi);
+    }
+    return __ldg(a.aux + k + (size_t)NUA * ((size_t)si + (size_t)a.mx * (size_t)sj));
 }
 
 // Exact double <-> float conversions done with integer operations.  On
@@ -152,7 +181,9 @@ struct TileCfg;
 GCLAW_TILE_CFG(RpAcoustics, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_TILE_F64_NT)
 GCLAW_TILE_CFG(RpShallow, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_TILE_F64_NT)
 GCLAW_TILE_CFG(RpEuler, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_TILE_F64_NT)
+GCLAW_TILE_CFG(RpVcAcoustics, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_TILE_F64_NT)
 #else
+GCLAW_TILE_CFG(RpVcAcoustics, double, 32, 16, 256)
 GCLAW_TILE_CFG(RpAcoustics, double, 32, 16, 256)
 GCLAW_TILE_CFG(RpShallow, double, 32, 16, 256)
 GCLAW_TILE_CFG(RpEuler, double, 16, 16, 256)
@@ -161,7 +192,9 @@ GCLAW_TILE_CFG(RpEuler, double, 16, 16, 256)
 GCLAW_TILE_CFG(RpAcoustics, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_TILE_F32_NT)
 GCLAW_TILE_CFG(RpShallow, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_TILE_F32_NT)
 GCLAW_TILE_CFG(RpEuler, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_TILE_F32_NT)
+GCLAW_TILE_CFG(RpVcAcoustics, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_TILE_F32_NT)
 #else
+GCLAW_TILE_CFG(RpVcAcoustics, float, 32, 16, 512)
 GCLAW_TILE_CFG(RpAcoustics, float, 32, 16, 512)
 GCLAW_TILE_CFG(RpShallow, float, 32, 16, 512)
 GCLAW_TILE_CFG(RpEuler, float, 24, 16, 384)
@@ -179,6 +212,10 @@ static inline void tile_shape(int rp, int precision, int *tx, int *ty) {
     case GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D:
         *tx = f64 ? TileCfg<RpShallow, double>::TX : TileCfg<RpShallow, float>::TX;
         *ty = f64 ? TileCfg<RpShallow, double>::TY : TileCfg<RpShallow, float>::TY;
+        return;
+    case GCLAW_RP_VC_ACOUSTICS_2D:
+        *tx = f64 ? TileCfg<RpVcAcoustics, double>::TX : TileCfg<RpVcAcoustics, float>::TX;
+        *ty = f64 ? TileCfg<RpVcAcoustics, double>::TY : TileCfg<RpVcAcoustics, float>::TY;
         return;
     default:
         *tx = f64 ? TileCfg<RpEuler, double>::TX : TileCfg<RpEuler, float>::TX;
@@ -249,6 +286,7 @@ struct Tile {
 // ---- phase 0: per-cell square roots and quotients for one sweep ---------
 template <class RP, typename T, int IXY, int TX, int TY, int NT>
 __device__ __forceinline__ void phase_aux(const typename RP::Params &P, const T *QS, T *CA) {
+    static_assert(RP::NUA == 0 || RP::NUA == RP::NA, "user aux is transformed in the aux area");
     using TL = Tile<RP, TX, TY>;
     constexpr int M = RP::M, NA = RP::NA;
     if (NA == 0) return;
@@ -262,7 +300,14 @@ __device__ __forceinline__ void phase_aux(const typename RP::Params &P, const T 
         T q[M], aux[NA > 0 ? NA : 1];
 #pragma unroll
         for (int k = 0; k < M; k++) q[k] = QS[k * TL::QN + c];
-        RP::cell_aux(P, q, aux);
+        if constexpr (RP::NUA > 0) {
+            // the user aux was loaded into CA with the tile; transform in place
+#pragma unroll
+            for (int f = 0; f < NA; f++) aux[f] = CA[f * TL::QN + c];
+            RP::cell_aux_user(P, q, aux);
+        } else {
+            RP::cell_aux(P, q, aux);
+        }
 #pragma unroll
         for (int f = 0; f < NA; f++) CA[f * TL::QN + c] = aux[f];
     }
@@ -298,7 +343,21 @@ __device__ __forceinline__ void phase_rpn2(const typename RP::Params &P, const T
             ar[f] = CA[f * TL::QN + cr];
         }
         T W[MW * M], s[MW], am[M], ap[M], R[NR > 0 ? NR : 1];
-        bad |= RP::template rpn2<IXY>(P, ql, qr, al, ar, W, s, am, ap, R);
+        if constexpr (RP::TNB) {
+            // aux of the cells below / above the two edge cells (transverse)
+            constexpr int TS = (IXY == 1) ? TL::QW : 1;
+            T bl[NA], tl[NA], br[NA], tr[NA];
+#pragma unroll
+            for (int f = 0; f < NA; f++) {
+                bl[f] = CA[f * TL::QN + cl - TS];
+                tl[f] = CA[f * TL::QN + cl + TS];
+                br[f] = CA[f * TL::QN + cr - TS];
+                tr[f] = CA[f * TL::QN + cr + TS];
+            }
+            bad |= RP::template rpn2_nb<IXY>(P, ql, qr, al, ar, bl, tl, br, tr, W, s, am, ap, R);
+        } else {
+            bad |= RP::template rpn2<IXY>(P, ql, qr, al, ar, W, s, am, ap, R);
+        }
 #pragma unroll
         for (int f = 0; f < MW * M; f++)
             if (RP::template wnz<IXY>(f / M, f % M))
@@ -412,8 +471,13 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
             T R[NR > 0 ? NR : 1];
 #pragma unroll
             for (int r = 0; r < NR; r++) R[r] = EA[(TL::FR + r) * TL::NE1 + ie];
-            RP::template rpt2<IXY>(P, R, am, bmm, bpm);
-            RP::template rpt2<IXY>(P, R, ap, bmp, bpp);
+            if constexpr (RP::TNB) {
+                RP::template rpt2s<IXY, 0>(P, R, am, bmm, bpm);
+                RP::template rpt2s<IXY, 1>(P, R, ap, bmp, bpp);
+            } else {
+                RP::template rpt2<IXY>(P, R, am, bmm, bpm);
+                RP::template rpt2<IXY>(P, R, ap, bmp, bpp);
+            }
         } else {
 #pragma unroll
             for (int k = 0; k < M; k++) bmm[k] = bpm[k] = bmp[k] = bpp[k] = (T)0;
@@ -534,7 +598,7 @@ static __device__ void finish_step(gclaw_ctrl *c, int ctrl_mode, double dt, doub
 // each value goes through the boundary conditions (load_q).
 template <class RP, typename T, int TX, int TY, int NT>
 __device__ __forceinline__ void load_tile(const StepArgs &a, const double *__restrict__ qin, int i0,
-                                          int j0, T *QS) {
+                                          int j0, T *QS, T *CA = nullptr) {
     using TL = Tile<RP, TX, TY>;
     constexpr int M = RP::M;
     const int off = a.ghosted ? 2 : 0, nx = a.mx + 2 * off, ny = a.my + 2 * off;
@@ -556,6 +620,15 @@ __device__ __forceinline__ void load_tile(const StepArgs &a, const double *__res
             const int cx = cell % (TX + 4), cy = cell / (TX + 4);
             QS[k * TL::QN + cy * TL::QW + cx] =
                 from_double<T>(load_q<M>(a, qin, k, i0 - 2 + cx, j0 - 2 + cy));
+        }
+    }
+    if constexpr (RP::NUA > 0) {
+        // user aux of the tile and its halo, into the per-cell aux area
+        for (int idx = threadIdx.x; idx < (TX + 4) * TL::QH * RP::NUA; idx += NT) {
+            const int k = idx % RP::NUA, cell = idx / RP::NUA;
+            const int cx = cell % (TX + 4), cy = cell / (TX + 4);
+            CA[k * TL::QN + cy * TL::QW + cx] =
+                from_double<T>(load_a<RP::NUA>(a, k, i0 - 2 + cx, j0 - 2 + cy));
         }
     }
 }
@@ -582,10 +655,12 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, const typename RPT<
     T *EB = EA + TL::EAW * TL::NE1;
     constexpr bool AUX1 = TL::template aux_own<T>();  // aux once per tile
     static_assert(AUX1 || RP::NA * TL::QN <= TL::EBW * TL::NE2, "cell aux area does not fit");
+    static_assert(AUX1 || (RP::NUA == 0 && !RP::TNB),
+                  "user aux and transverse-neighbour aux need the per-tile aux area");
     T *CA = AUX1 ? EB + TL::EBW * TL::NE2 : EB;
     const T tdtdx = (T)dtdx, tdtdy = (T)dtdy;
 
-    load_tile<RP, T, TX, TY, NT>(a, qin, i0, j0, QS);
+    load_tile<RP, T, TX, TY, NT>(a, qin, i0, j0, QS, CA);
     __syncthreads();
 
     A acc[NC][M];

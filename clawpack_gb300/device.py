@@ -21,7 +21,7 @@ def _stream_handle(stream=None):
 
 
 def make_solver_struct(rp_id, mx, my, dx, dy, bc_lower, bc_upper, mthlim, order, tw,
-                       precision, problem_data):
+                       precision, problem_data, aux_bc_lower=(1, 1), aux_bc_upper=(1, 1)):
     s = _lib.GclawSolver()
     s.rp = int(rp_id)
     s.mx, s.my = int(mx), int(my)
@@ -38,6 +38,9 @@ def make_solver_struct(rp_id, mx, my, dx, dy, bc_lower, bc_upper, mthlim, order,
     pd = list(problem_data) + [0.0] * (8 - len(problem_data))
     for i in range(8):
         s.problem_data[i] = float(pd[i])
+    for d in range(2):
+        s.aux_bc_lower[d] = int(aux_bc_lower[d])
+        s.aux_bc_upper[d] = int(aux_bc_upper[d])
     return s
 
 
@@ -46,16 +49,19 @@ class DeviceProblem:
     ``split=True`` steps are dimensionally split (x-sweep, then y-sweep) and a
     third buffer holds the state between the sweeps."""
 
-    def __init__(self, solver_struct, device=None, strict=False, split=False):
+    def __init__(self, solver_struct, device=None, strict=False, split=False, aux=None):
         self.s = solver_struct
         self.L = L = _lib.lib(strict)
+        self.device = torch.device(device or "cuda")
+        self.aux = None
+        if aux is not None:
+            self.set_aux(aux)
         _lib.check(L.gclaw_check(ctypes.byref(self.s)), "gclaw_check")
         m = ctypes.c_int()
         mw = ctypes.c_int()
         _lib.check(L.gclaw_rp_shape(self.s.rp, ctypes.byref(m), ctypes.byref(mw)))
         self.m, self.mw = m.value, mw.value
         self.mx, self.my = self.s.mx, self.s.my
-        self.device = torch.device(device or "cuda")
         shape = (self.my, self.mx, self.m)
         self.q = [torch.empty(shape, dtype=torch.float64, device=self.device),
                   torch.empty(shape, dtype=torch.float64, device=self.device)]
@@ -65,6 +71,17 @@ class DeviceProblem:
         self.ctrl = torch.zeros(256, dtype=torch.uint8, device=self.device)
         self._ctrl_host = torch.empty(256, dtype=torch.uint8, pin_memory=True)
         self.ctrl_init(0.0, 1.0, 0.0)
+
+    def set_aux(self, aux):
+        """Copy a host (num_aux, mx, my) aux array to the device and point the
+        solver description at it (solvers with an aux array)."""
+        af = np.asfortranarray(aux, dtype=np.float64)
+        if af.shape[1:] != (self.s.mx, self.s.my):
+            raise ValueError(f"aux has shape {af.shape}, expected (num_aux, {self.s.mx}, "
+                             f"{self.s.my})")
+        t = torch.from_numpy(af.T.copy()).to(self.device)
+        self.aux = t  # keeps the device array alive while the struct points at it
+        self.s.aux = t.data_ptr()
 
     # -- host <-> device ---------------------------------------------------
     def upload(self, q, buf=0):

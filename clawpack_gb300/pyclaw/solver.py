@@ -84,6 +84,8 @@ class ClawSolver2D:
         self.dt_variable = True
         self.bc_lower = [None, None]
         self.bc_upper = [None, None]
+        self.aux_bc_lower = [None, None]
+        self.aux_bc_upper = [None, None]
         self.reflect_index = [1, 2]
         self.device_control = True
         self.batch = 32
@@ -119,6 +121,8 @@ class ClawSolver2D:
             return [rho, bulk, cc, zz]
         if rp == _lib.RP_SHALLOW_ROE_WITH_EFIX_2D:
             return [float(pd["grav"])]
+        if rp == _lib.RP_VC_ACOUSTICS_2D:
+            return []  # the medium is in state.aux
         return [float(pd["gamma"]), 1.0 if pd.get("efix", True) else 0.0]
 
     def _check_options(self, state):
@@ -132,8 +136,22 @@ class ClawSolver2D:
             raise NotImplementedError("fwave, step_source and before_step are not supported")
         if self.num_ghost != 2:
             raise ValueError("num_ghost must be 2")
-        if state.num_aux:
-            raise NotImplementedError("aux arrays are not supported")
+        need_aux = getattr(self.rp, "num_aux", 0)
+        if state.num_aux != need_aux:
+            raise ValueError(f"{self.rp.name} needs num_aux = {need_aux}, the state has "
+                             f"{state.num_aux}")
+        if need_aux:
+            if state.aux is None:
+                raise ValueError("state.aux is not set")
+            if self.dimensional_split:
+                raise NotImplementedError("dimensional splitting with an aux array is not "
+                                          "supported; set solver.dimensional_split = False")
+            for b in list(self.aux_bc_lower) + list(self.aux_bc_upper):
+                if b is None:
+                    raise ValueError("aux boundary conditions are not set (solver.aux_bc_lower, "
+                                     "solver.aux_bc_upper)")
+                if b == BC.custom:
+                    raise NotImplementedError("BC.custom is not supported by the CUDA backend")
         for b in list(self.bc_lower) + list(self.bc_upper):
             if b is None:
                 raise ValueError("boundary conditions are not set")
@@ -149,9 +167,11 @@ class ClawSolver2D:
         mx, my = g.num_cells
         dx, dy = g.delta
         prec = _lib.PREC_FP64 if self.precision == "fp64" else _lib.PREC_FP32_BULK
+        abl = self.aux_bc_lower if state.num_aux else (1, 1)
+        abu = self.aux_bc_upper if state.num_aux else (1, 1)
         return make_solver_struct(self.rp.rp_id, mx, my, dx, dy, self.bc_lower, self.bc_upper,
                                   self._mthlim, self.order, self.transverse_waves, prec,
-                                  self._problem_data(state))
+                                  self._problem_data(state), abl, abu)
 
     def setup(self, solution):
         self._check_options(solution.state)
@@ -164,8 +184,10 @@ class ClawSolver2D:
         split = bool(self.dimensional_split)
         key = (bytes(s), split)
         if self._dev is None or self._dev_key != key:
-            self._dev = DeviceProblem(s, split=split)
+            self._dev = DeviceProblem(s, split=split, aux=state.aux if state.num_aux else None)
             self._dev_key = key
+        elif state.num_aux:
+            self._dev.set_aux(state.aux)  # the caller may have changed the medium
         return self._dev
 
     # ------------------------------------------------------------------ stepping

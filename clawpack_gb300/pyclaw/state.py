@@ -18,14 +18,13 @@ class State:
             self.patch = geom
         else:
             raise TypeError("State(domain_or_patch, num_eqn)")
-        if num_aux:
-            raise NotImplementedError("aux arrays are not supported by this backend")
         self.num_eqn = int(num_eqn)
-        self.num_aux = 0
+        self.num_aux = int(num_aux)
         self.problem_data = {}
         self.t = 0.0
         self.q = np.zeros([self.num_eqn] + self.patch.grid.num_cells, order="F")
-        self.aux = None
+        self.aux = (np.zeros([self.num_aux] + self.patch.grid.num_cells, order="F")
+                    if self.num_aux else None)
 
     @property
     def grid(self):
@@ -36,7 +35,7 @@ class State:
         return self.patch.num_dim
 
     def __setattr__(self, name, value):
-        if name == "q":
+        if name == "q" or (name == "aux" and value is not None):
             value = np.asfortranarray(value, dtype=np.float64)
         object.__setattr__(self, name, value)
 

@@ -20,12 +20,15 @@ def _descriptor(name, rp_id):
     # PyClaw fills from state.problem_data before stepping.
     return SimpleNamespace(__name__=f"clawpack_gb300.riemann.{name}", name=name, rp_id=rp_id,
                            num_eqn=static.num_eqn[name], num_waves=static.num_waves[name],
-                           cparam=SimpleNamespace())
+                           num_aux=static.num_aux[name], cparam=SimpleNamespace())
 
 
 acoustics_2D = _descriptor("acoustics_2D", _lib.RP_ACOUSTICS_2D)
 shallow_roe_with_efix_2D = _descriptor("shallow_roe_with_efix_2D",
                                        _lib.RP_SHALLOW_ROE_WITH_EFIX_2D)
 euler_4wave_2D = _descriptor("euler_4wave_2D", _lib.RP_EULER_4WAVE_2D)
+# variable-coefficient acoustics: state.aux = (rho, c) per cell
+vc_acoustics_2D = _descriptor("vc_acoustics_2D", _lib.RP_VC_ACOUSTICS_2D)
 
-__all__ = ["acoustics_2D", "shallow_roe_with_efix_2D", "euler_4wave_2D", "static"]
+__all__ = ["acoustics_2D", "shallow_roe_with_efix_2D", "euler_4wave_2D", "vc_acoustics_2D",
+           "static"]

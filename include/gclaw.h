@@ -34,6 +34,7 @@ extern "C" {
 #define GCLAW_RP_ACOUSTICS_2D 1             /* m=3 (p,u,v), 2 waves; pd: rho, bulk, cc, zz */
 #define GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D 2 /* m=3 (h,hu,hv), 3 waves; pd: grav */
 #define GCLAW_RP_EULER_4WAVE_2D 3           /* m=4 (rho,rhou,rhov,E), 4 waves; pd: gamma, efix */
+#define GCLAW_RP_VC_ACOUSTICS_2D 4          /* m=3 (p,u,v), 2 waves; aux (rho, c) per cell */
 
 /* Boundary conditions: the values of pyclaw.BC. */
 #define GCLAW_BC_CUSTOM 0 /* not supported: rejected with GCLAW_ERR_UNSUPPORTED */
@@ -77,6 +78,14 @@ typedef struct gclaw_solver {
     int transverse_waves;         /* 0, 1 or 2 (solver.transverse_waves) */
     int precision;                /* GCLAW_PREC_* */
     double problem_data[8];       /* state.problem_data, layout per GCLAW_RP_* */
+    /* Solvers with an aux array (GCLAW_RP_VC_ACOUSTICS_2D): device pointer to
+     * aux, laid out like q with maux = 2 components -- (maux, mx, my), or
+     * (maux, mx+4, my+4) with ghost cells filled for gclaw_step2 -- and its
+     * boundary conditions (state.aux; solver.aux_bc_lower / aux_bc_upper;
+     * walls mirror without negation).  Ignored by the other solvers; a
+     * zero-initialised tail means "no aux". */
+    const double *aux;
+    int aux_bc_lower[2], aux_bc_upper[2];
 } gclaw_solver;
 
 /* Time-step control block, resident in device memory.  The step kernel's

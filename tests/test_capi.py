@@ -40,7 +40,9 @@ def _offsets_from_header(struct_name):
         decl = decl.strip()
         if not decl:
             continue
-        typ, rest = re.match(r"((?:unsigned\s+)?(?:long\s+long|int|double))\s+(.*)", decl).groups()
+        typ, rest = re.match(
+            r"((?:const\s+)?(?:unsigned\s+)?(?:long\s+long|int|double))\s*\*?\s*(.*)",
+            decl).groups()
         for item in rest.split(","):
             item = item.strip()
             m = re.match(r"([a-z_0-9]+)(?:\[([A-Z_0-9]+)\])?", item)
@@ -115,3 +117,17 @@ def test_noalloc_refuses_oversized_grids_before_any_cuda_call():
             assert L.gclaw_step2_noalloc(ctypes.byref(s), None, None, 1e-5, ctypes.byref(cfl),
                                          None) == _lib.ERR_TOO_LARGE
             assert cfl.value == -1.0
+
+
+def test_aux_solver_needs_aux_pointer_and_aux_bcs():
+    L = _lib.lib()
+    s = make_solver_struct(_lib.RP_VC_ACOUSTICS_2D, 8, 8, 0.1, 0.1, [1, 1], [1, 1], [4, 4], 2, 2,
+                           0, [])
+    assert L.gclaw_check(ctypes.byref(s)) == _lib.ERR_ARG  # no aux array
+    s.aux = 0x100000  # any non-null device address passes the host check
+    assert L.gclaw_check(ctypes.byref(s)) == 0
+    s.aux_bc_lower[0] = 2  # periodic on one side only
+    assert L.gclaw_check(ctypes.byref(s)) == _lib.ERR_ARG
+    m, mw = ctypes.c_int(), ctypes.c_int()
+    assert L.gclaw_rp_shape(_lib.RP_VC_ACOUSTICS_2D, ctypes.byref(m), ctypes.byref(mw)) == 0
+    assert (m.value, mw.value) == (3, 2)
