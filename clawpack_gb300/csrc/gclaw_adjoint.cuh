@@ -113,21 +113,25 @@ struct AdjShallow {
     __device__ __forceinline__ static void cell_aux_adj(const typename RP::Params &P,
                                                         const T *q, const T *aux, const T *auxb,
                                                         T *qb) {
+        // one reciprocal of sqrt(h), of h and of sqrt(g h) instead of a
+        // quotient per term (the derivative of each aux value is linear in
+        // these)
         const T h = q[0], hs = aux[0];
+        const T ihs = (T)1 / hs, ih = (T)1 / h, ic = (T)1 / aux[5];
         // hu/hs, hv/hs
         T hsb = auxb[0];
-        qb[1] += auxb[1] / hs;
-        hsb -= auxb[1] * aux[1] / hs;
-        qb[2] += auxb[2] / hs;
-        hsb -= auxb[2] * aux[2] / hs;
+        qb[1] += auxb[1] * ihs;
+        hsb -= auxb[1] * aux[1] * ihs;
+        qb[2] += auxb[2] * ihs;
+        hsb -= auxb[2] * aux[2] * ihs;
         // hu/h, hv/h
-        qb[1] += auxb[3] / h;
-        qb[2] += auxb[4] / h;
-        T hb = -(auxb[3] * aux[3] + auxb[4] * aux[4]) / h;
+        qb[1] += auxb[3] * ih;
+        qb[2] += auxb[4] * ih;
+        T hb = -(auxb[3] * aux[3] + auxb[4] * aux[4]) * ih;
         // sqrt(g h)
-        hb += auxb[5] * P.g / ((T)2 * aux[5]);
+        hb += auxb[5] * P.g * (T)0.5 * ic;
         // sqrt(h)
-        hb += hsb / ((T)2 * hs);
+        hb += hsb * (T)0.5 * ihs;
         qb[0] += hb;
     }
 
@@ -154,18 +158,24 @@ struct AdjShallow {
         if (!allright) {
             h1 = hl + W[0];
             hu1 = ql[mu] + W[mu];
-            g1sq = sqrt(g * h1);
-            s1 = hu1 / h1 - g1sq;
-            trans1 = (s0 < (T)0 && s1 > (T)0);
+            // the intermediate speeds only where the forward's exact pre-test
+            // leaves the transonic case open (the same branch decisions)
+            if (lt0(s0) && !no_right_sonic_point(h1, hu1, g)) {
+                g1sq = sqrt(g * h1);
+                s1 = hu1 / h1 - g1sq;
+                trans1 = s1 > (T)0;
+            }
             sf1 = trans1 ? s0 * (s1 - s[0]) / (s1 - s0) : (s[0] < (T)0 ? s[0] : (T)0);
             go2 = s[1] < (T)0;
             if (go2) {
                 s03 = ar[2 + mu] + ar[5];
                 h3 = hr - W[6];
                 hu3 = qr[mu] - W[6 + mu];
-                g3sq = sqrt(g * h3);
-                s3 = hu3 / h3 + g3sq;
-                trans3 = (s3 < (T)0 && s03 > (T)0);
+                if (gt0(s03) && !no_right_sonic_point(h3, -hu3, g)) {
+                    g3sq = sqrt(g * h3);
+                    s3 = hu3 / h3 + g3sq;
+                    trans3 = s3 < (T)0;
+                }
                 add3 = trans3 || s[2] < (T)0;
                 sf3 = trans3 ? s3 * (s03 - s[2]) / (s03 - s3) : s[2];
             }
@@ -294,16 +304,19 @@ struct AdjShallow {
         qlb[mv] -= d2b;
         // Roe state: half = 0.5 / c; c = sqrt(g hbar); hbar = (hl + hr) / 2;
         // u = (us_l + us_r) / S, v = (vs_l + vs_r) / S, S = hs_l + hs_r
-        cb -= halfb * half / c;
-        const T hbarb = cb * g / ((T)2 * c);
+        // 1 / c = 2 half; one reciprocal of S
+        cb -= halfb * half * ((T)2 * half);
+        const T hbarb = cb * g * half;
         qlb[0] += (T)0.5 * hbarb;
         qrb[0] += (T)0.5 * hbarb;
         const T S = al[0] + ar[0];
-        const T Sb = -(ub * u + vb * v) / S;
-        alb[mu] += ub / S;
-        arb[mu] += ub / S;
-        alb[mv] += vb / S;
-        arb[mv] += vb / S;
+        const T iS = (T)1 / S;
+        const T Sb = -(ub * u + vb * v) * iS;
+        const T ubS = ub * iS, vbS = vb * iS;
+        alb[mu] += ubS;
+        arb[mu] += ubS;
+        alb[mv] += vbS;
+        arb[mv] += vbS;
         alb[0] += Sb;
         arb[0] += Sb;
     }
