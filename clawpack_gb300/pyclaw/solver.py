@@ -132,8 +132,10 @@ class ClawSolver2D:
             raise NotImplementedError(
                 f"kernel_language={self.kernel_language!r}: this framework provides the 'CUDA' "
                 "backend only")
-        if self.fwave or self.step_source is not None or self.before_step is not None:
-            raise NotImplementedError("fwave, step_source and before_step are not supported")
+        if self.fwave:
+            raise NotImplementedError("fwave is not supported")
+        if self.step_source is not None and self.source_split not in (1, 2):
+            raise ValueError("solver.source_split must be 1 (Godunov) or 2 (Strang)")
         if self.num_ghost != 2:
             raise ValueError("num_ghost must be 2")
         need_aux = getattr(self.rp, "num_aux", 0)
@@ -191,9 +193,9 @@ class ClawSolver2D:
         return self._dev
 
     # ------------------------------------------------------------------ stepping
-    def step(self, solution, take_one_step=False, tstart=None, tend=None):
-        """One step of size self.dt (PyClaw's step_hyperbolic): the fused
-        ghost fill + classic step on the GPU; sets state.q and self.cfl."""
+    def step_hyperbolic(self, solution):
+        """One hyperbolic step of size self.dt: the fused ghost fill + classic
+        step on the GPU; sets state.q and returns the Courant number."""
         state = solution.state
         dev = self._device(state)
         dev.upload(state.q, 0)
@@ -202,6 +204,19 @@ class ClawSolver2D:
         _lib.check(c.status, "step")
         self.cfl.update_global_max(c.cfl)
         state.q = dev.download(1)
+        return c.cfl
+
+    def step(self, solution, take_one_step=False, tstart=None, tend=None):
+        """One step of size self.dt with PyClaw's source splitting:
+        step_source(solver, state, dt) after the hyperbolic step
+        (source_split 1, Godunov) or half steps before and after it
+        (source_split 2, Strang); sets state.q and self.cfl."""
+        state = solution.state
+        if self.step_source is not None and self.source_split == 2:
+            self.step_source(self, state, self.dt / 2.0)
+        self.step_hyperbolic(solution)
+        if self.step_source is not None:
+            self.step_source(self, state, self.dt if self.source_split == 1 else self.dt / 2.0)
         return True
 
     def evolve_to_time(self, solution, tend=None):
@@ -221,6 +236,8 @@ class ClawSolver2D:
 
     def _evolve(self, solution, tend, max_accepted):
         state = solution.state
+        if self.step_source is not None or self.before_step is not None:
+            return self._evolve_hooked(solution, tend, max_accepted)
         dev = self._device(state)
         dev.upload(state.q, 0)
         if self.device_control:
@@ -244,6 +261,61 @@ class ClawSolver2D:
         self.status["dtmin"] = min(self.status["dtmin"], dtmin)
         self.status["dtmax"] = max(self.status["dtmax"], dtmax)
         self.logger.debug("evolve to t=%g: %d steps, last dt=%g, cfl=%g", t, numsteps, dt, cfl)
+        _lib.check(status, "evolve_to_time")
+        return self.status
+
+    def _evolve_hooked(self, solution, tend, max_accepted):
+        """evolve_to_time with Python hooks (before_step, step_source): the
+        hooks see state.q as a host array, so every attempt runs on the host:
+        before_step, step() (source splitting around the GPU step), then the
+        CFL check, which restores the state of the start of the step on
+        rejection (upstream pyclaw/src/pyclaw/solver.py)."""
+        state = solution.state
+        t, dt = solution.t, self.dt
+        tstart = t
+        numsteps = 0
+        cflmax = 0.0
+        dtmin = dtmax = dt
+        status = _lib.MAX_STEPS
+        for _ in range(self.max_steps):
+            if t + dt > tend and tstart < tend:
+                dt = tend - t
+            if tend - t - dt < 1.0e-14 * t:
+                dt = tend - t
+            q_backup = state.q.copy(order="F")
+            state.t = t
+            if self.before_step is not None:
+                self.before_step(self, state)
+            self.dt = dt
+            self.step(solution)
+            cfl = self.cfl.get_cached_max()
+            if cfl <= self.cfl_max:
+                cflmax = max(cfl, cflmax)
+                numsteps += 1
+                t = t + dt if self.dt_variable else tstart + numsteps * dt
+            else:
+                state.q = q_backup
+                if not self.dt_variable:
+                    status = _lib.CFL_FIXED_DT
+                    break
+            if t >= tend or (max_accepted >= 0 and numsteps >= max_accepted):
+                status = _lib.OK
+                break
+            if self.dt_variable:
+                if cfl > 0.0:
+                    dt = min(self.dt_max, dt * self.cfl_desired / cfl)
+                    dtmin = min(dt, dtmin)
+                    dtmax = max(dt, dtmax)
+                else:
+                    dt = self.dt_max
+        solution.t = t
+        state.t = t
+        self.dt = dt
+        self.status["numsteps"] += numsteps
+        if numsteps:
+            self.status["cflmax"] = max(self.status["cflmax"], cflmax)
+        self.status["dtmin"] = min(self.status["dtmin"], dtmin)
+        self.status["dtmax"] = max(self.status["dtmax"], dtmax)
         _lib.check(status, "evolve_to_time")
         return self.status
 
