@@ -519,6 +519,25 @@ __device__ __forceinline__ void phase_accum(const T *EA, const T *EB, A (*acc)[R
             const T *BMM = EB + (TL::GMM + k) * TL::NE2, *BPM = EB + (TL::GPM + k) * TL::NE2;
             const T *BMP = EB + (TL::GMP + k) * TL::NE2, *BPP = EB + (TL::GPP + k) * TL::NE2;
             const T *FA = EB + (TL::GFA + k) * TL::NE2;
+#ifndef GCLAW_STRICT
+            // FP64: the same terms regrouped: the first-order and correction
+            // parts share the factor dt/dn and the eight transverse parts the
+            // factor (dt/dt') h, so the cell takes two multiply-adds instead of
+            // the reference's term-by-term sequence (GCLAW_STRICT keeps that;
+            // in FP32 the longer-lived sums cost a register spill, so FP32
+            // keeps it too).
+            if constexpr (sizeof(T) == 8) {
+                const T s1 = (EA[(TL::FAP + k) * TL::NE1 + el] + EA[(TL::FAM + k) * TL::NE1 + er]) +
+                             (FA[o0 + S2] - FA[o0]);
+                const T tb = ((BPM[b0 + S2] + BPP[b0]) - (BPM[o0 + S2] + BPP[o0])) +
+                             ((BMM[o0 + S2] + BMP[o0]) - (BMM[a0 + S2] + BMP[a0]));
+                A v = acc[t][k];
+                v = v - (A)dtdn * (A)s1;
+                v = v - (A)(dtdt * h) * (A)tb;
+                acc[t][k] = v;
+                continue;
+            }
+#endif
             const T g2b = ((T)0 - h * BPM[b0 + S2]) - h * BPP[b0];
             const T qo = ((T)0 - dtdn * EA[(TL::FAP + k) * TL::NE1 + el]) -
                          dtdn * EA[(TL::FAM + k) * TL::NE1 + er];
