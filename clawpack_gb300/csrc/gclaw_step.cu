@@ -100,6 +100,8 @@ __global__ void __launch_bounds__(STRIP_NW * 32, GCLAW_STRIP_BLOCKS(RPT))
     strip_kernel(const StepArgs a, const typename RPT<float>::Params P, int seg_rows, int nstrips,
                  int nunits) {
     constexpr int NT = STRIP_NW * 32;
+    constexpr bool RING = StripCfg<RPT>::RING;
+    extern __shared__ __align__(16) unsigned char strip_smem[];
     __shared__ double s_dt, s_dtdx, s_dtdy;
     __shared__ int s_par, s_skip;
     __shared__ float s_red[2][STRIP_NW];
@@ -133,8 +135,11 @@ __global__ void __launch_bounds__(STRIP_NW * 32, GCLAW_STRIP_BLOCKS(RPT))
     if (unit < nunits) {
         const int strip = unit % nstrips, seg = unit / nstrips;
         const int j0 = seg * seg_rows, j1 = min(j0 + seg_rows, a.my);
-        strip_run<RPT>(a, P, qin, qout, (float)dtdx, (float)dtdy, lane, strip * STRIP_W + lane - 2,
-                       j0, j1, smax_x, smax_y, bad);
+        float *ring = RING ? reinterpret_cast<float *>(strip_smem) +
+                                 (threadIdx.x >> 5) * 32 * strip_ring_floats<RPT<float>>()
+                           : nullptr;
+        strip_run<RPT, RING>(a, P, qin, qout, (float)dtdx, (float)dtdy, lane,
+                             strip * STRIP_W + lane - 2, j0, j1, smax_x, smax_y, bad, ring);
     }
 
     const int anybad = block_reduce<float, NT>(smax_x, smax_y, bad, s_red);
@@ -205,21 +210,28 @@ static int launch_tile(const gclaw_solver *s, const StepArgs &a, cudaStream_t st
 }
 
 // FP32-bulk kernel family: 0 = per-solver default, 1 = tiles, 2 = strips.
-// The default is the faster family on GB300 at 2048^2: strips for
-// acoustics (20.6 vs 14.4 Gcell-updates/s), tiles for shallow water (equal
-// speed) and Euler (7.2 vs 7.1, the strip kernel needing 255 registers).
+// The default is the faster family on GB300 at 2048^2: strips for all three
+// solvers (acoustics 21.3 vs 14.0, shallow water 14.2 vs 12.2, Euler 9.1 vs
+// 7.0 Gcell-updates/s); solvers that read transverse-neighbour aux run on
+// tiles.
 static int g_fp32_kernel = 0;
 
 template <template <typename> class RPT>
 static int launch_strip(const gclaw_solver *s, const StepArgs &a, cudaStream_t st, int nlaunch) {
     auto kern = strip_kernel<RPT>;
+    constexpr size_t smem =
+        StripCfg<RPT>::RING ? sizeof(float) * STRIP_NW * 32 * strip_ring_floats<RPT<float>>() : 0;
     static int warp_slots[32] = {0};  // resident warps per GPU, per device ordinal < 32
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return GCLAW_ERR_CUDA;
     int slots = dev < 32 ? warp_slots[dev] : 0;
     if (slots == 0) {
         int nb = 0, nsm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, STRIP_NW * 32, 0) !=
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess)
+            return GCLAW_ERR_CUDA;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, STRIP_NW * 32, smem) !=
                 cudaSuccess ||
             cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
             return GCLAW_ERR_CUDA;
@@ -238,7 +250,7 @@ static int launch_strip(const gclaw_solver *s, const StepArgs &a, cudaStream_t s
     const int nblocks = (nunits + STRIP_NW - 1) / STRIP_NW;
     const typename RPT<float>::Params P = RPT<float>::make(s->problem_data);
     for (int l = 0; l < nlaunch; l++)
-        kern<<<nblocks, STRIP_NW * 32, 0, st>>>(a, P, seg_rows, nstrips, nunits);
+        kern<<<nblocks, STRIP_NW * 32, smem, st>>>(a, P, seg_rows, nstrips, nunits);
     return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
 }
 
@@ -247,9 +259,9 @@ static bool strip_default();
 template <>
 bool strip_default<RpAcoustics>() { return true; }
 template <>
-bool strip_default<RpShallow>() { return false; }
+bool strip_default<RpShallow>() { return true; }
 template <>
-bool strip_default<RpEuler>() { return false; }
+bool strip_default<RpEuler>() { return true; }
 
 template <template <typename> class RPT, typename T>
 static int launch_cfg(const gclaw_solver *s, const StepArgs &a, cudaStream_t st, int nlaunch) {

@@ -42,16 +42,32 @@ constexpr int STRIP_NW = GCLAW_STRIP_NW;  // warps per block
 constexpr int STRIP_MIN_ROWS = 16;
 
 // Resident blocks per SM the kernel is compiled for (the register budget):
-// acoustics fits 128 registers, the Roe solvers get 168 (measured best on
-// GB300 among 1-4 blocks of 2-8 warps).
+// acoustics and shallow water fit 128 registers, Euler gets 168.
+// RING: keep the y-edge records and the saved limited-edge terms in this
+// warp's shared memory (three slots rotating with the rows, lane-fastest,
+// each lane touching only its own column's slots) instead of registers, for
+// solvers whose records would not leave room for enough resident warps.
 template <template <typename> class RPT>
 struct StripCfg {
     static constexpr int MINB = 3;
+    static constexpr bool RING = true;
 };
 template <>
 struct StripCfg<RpAcoustics> {
     static constexpr int MINB = 4;
+    static constexpr bool RING = false;
 };
+template <>
+struct StripCfg<RpShallow> {
+    static constexpr int MINB = 4;  // 127 registers with the ring, no spills
+    static constexpr bool RING = true;
+};
+
+// Floats of shared memory per lane for the y-edge ring of solver RP.
+template <class RP>
+__host__ __device__ constexpr int strip_ring_floats() {
+    return 3 * (RP::MW * RP::M + RP::MW + 2 * RP::M + (RP::NR > 0 ? RP::NR : 1)) + 4 * RP::M;
+}
 
 template <typename T>
 __device__ __forceinline__ T shfl_up1(T v) {
@@ -152,15 +168,61 @@ __device__ __forceinline__ void load_row(const StepArgs &a, const double *__rest
     for (int k = 0; k < RP::M; k++) qd[k] = load_q<RP::M>(a, qin, k, c, r);
 }
 
-// The march of one warp over rows [j0, j1) of its strip.
-template <template <typename> class RPT>
+// y-edge records in a warp's shared-memory ring: slot-major, field, lane.
+template <class RP>
+struct StripRing {
+    static constexpr int NW = RP::MW * RP::M, NR = RP::NR > 0 ? RP::NR : 1;
+    static constexpr int NF = NW + RP::MW + 2 * RP::M + NR;
+    float *base;  // this warp's area, lane-offset applied
+    __device__ __forceinline__ float &at(int slot, int f) const { return base[(slot * NF + f) * 32]; }
+    __device__ __forceinline__ float &lim(int f) const { return base[(3 * NF + f) * 32]; }
+    __device__ __forceinline__ void put(int slot, const StripEdge<RP> &e) const {
+#pragma unroll
+        for (int f = 0; f < NW; f++)
+            if (RP::template wnz<2>(f / RP::M, f % RP::M)) at(slot, f) = e.W[f];
+#pragma unroll
+        for (int p = 0; p < RP::MW; p++) at(slot, NW + p) = e.s[p];
+#pragma unroll
+        for (int k = 0; k < RP::M; k++) {
+            at(slot, NW + RP::MW + k) = e.am[k];
+            at(slot, NW + RP::MW + RP::M + k) = e.ap[k];
+        }
+#pragma unroll
+        for (int r = 0; r < NR; r++) at(slot, NW + RP::MW + 2 * RP::M + r) = e.R[r];
+    }
+    __device__ __forceinline__ void get(int slot, StripEdge<RP> &e) const {
+#pragma unroll
+        for (int f = 0; f < NW; f++)
+            e.W[f] = RP::template wnz<2>(f / RP::M, f % RP::M) ? at(slot, f) : 0.0f;
+#pragma unroll
+        for (int p = 0; p < RP::MW; p++) e.s[p] = at(slot, NW + p);
+#pragma unroll
+        for (int k = 0; k < RP::M; k++) {
+            e.am[k] = at(slot, NW + RP::MW + k);
+            e.ap[k] = at(slot, NW + RP::MW + RP::M + k);
+        }
+#pragma unroll
+        for (int r = 0; r < NR; r++) e.R[r] = at(slot, NW + RP::MW + 2 * RP::M + r);
+    }
+    __device__ __forceinline__ void get_w(int slot, float *W) const {
+#pragma unroll
+        for (int f = 0; f < NW; f++)
+            W[f] = RP::template wnz<2>(f / RP::M, f % RP::M) ? at(slot, f) : 0.0f;
+    }
+};
+
+// The march of one warp over rows [j0, j1) of its strip.  ring: this warp's
+// shared-memory area (strip_ring_floats per lane) when RING.
+template <template <typename> class RPT, bool RING>
 __device__ __forceinline__ void strip_run(const StepArgs &a, const typename RPT<float>::Params &P,
                                           const double *__restrict__ qin,
                                           double *__restrict__ qout, float dtdx, float dtdy,
                                           int lane, int c, int j0, int j1, float &smax_x,
-                                          float &smax_y, bool &bad) {
+                                          float &smax_y, bool &bad, float *ring) {
     using RP = RPT<float>;
     using T = float;
+    const StripRing<RP> yr{ring + lane};
+    int so = 0, sm = 1, sn = 2;  // ring slots of the y-edges r-5/2, r-3/2, r-1/2
     constexpr int M = RP::M, MW = RP::MW, NR = RP::NR > 0 ? RP::NR : 1;
     constexpr int NA = RP::NA > 0 ? RP::NA : 1;
     const int mthlim = a.mthlim, order = a.order, tw = a.tw;
@@ -261,6 +323,17 @@ __device__ __forceinline__ void strip_run(const StepArgs &a, const typename RPT<
                 }
             }
             if (r >= j0 + 1) {
+                if constexpr (RING) {
+                    yr.get(sm, Em);
+                    yr.get_w(so, Eo.W);
+#pragma unroll
+                    for (int k = 0; k < M; k++) {
+                        LAP[k] = yr.lim(k);
+                        LFA[k] = yr.lim(M + k);
+                        LBMP[k] = yr.lim(2 * M + k);
+                        LBPP[k] = yr.lim(3 * M + k);
+                    }
+                }
                 T W[MW * M];
 #pragma unroll
                 for (int f = 0; f < MW * M; f++) W[f] = Em.W[f];
@@ -302,10 +375,24 @@ __device__ __forceinline__ void strip_run(const StepArgs &a, const typename RPT<
                     LFA[k] = fa[k];
                     LBMP[k] = bmp[k];
                     LBPP[k] = bpp[k];
+                    if constexpr (RING) {
+                        yr.lim(k) = LAP[k];
+                        yr.lim(M + k) = LFA[k];
+                        yr.lim(2 * M + k) = LBMP[k];
+                        yr.lim(3 * M + k) = LBPP[k];
+                    }
                 }
             }
-            Eo = Em;
-            Em = En;
+            if constexpr (RING) {
+                yr.put(sn, En);
+                const int t = so;
+                so = sm;
+                sm = sn;
+                sn = t;
+            } else {
+                Eo = Em;
+                Em = En;
+            }
         }
 
         // ---- shift the row windows ---------------------------------------------
