@@ -66,8 +66,10 @@ __device__ __forceinline__ double load_q(const StepArgs &a, const double *__rest
         else if (b == GCLAW_BC_PERIODIC) si = gi - a.mx;
         else { si = 2 * a.mx - 1 - gi; neg = neg || (k == 1); }
     }
-    double v = __ldg(q + k + (size_t)M * ((size_t)si + (size_t)a.mx * (size_t)sj));
-    return neg ? -v : v;
+    const double v = __ldg(q + k + (size_t)M * ((size_t)si + (size_t)a.mx * (size_t)sj));
+    // sign flip on the integer pipes (a negation would be an FP64 instruction)
+    return __longlong_as_double(__double_as_longlong(v) ^
+                                (neg ? (long long)0x8000000000000000ull : 0ll));
 }
 
 // Component k of the ghost-filled aux array at (gi, gj), as load_q maps q but
@@ -103,6 +105,12 @@ __device__ __forceinline__ double load_a(const StepArgs &a, int k, int gi, int g
 // to double widening for zeros and normal numbers and fall back to the
 // instructions otherwise (denormals, very small or large magnitudes,
 // infinities, NaN).
+// The uncommon cases go through real calls, so that the compiler branches
+// around the conversion instruction instead of executing it for every value
+// and selecting.
+static __device__ __noinline__ float d2f_slow(double x) { return __double2float_rn(x); }
+static __device__ __noinline__ double f2d_slow(float x) { return (double)x; }
+
 __device__ __forceinline__ float d2f_rn_bits(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
@@ -114,7 +122,7 @@ __device__ __forceinline__ float d2f_rn_bits(double x) {
         f += (rem > 0x10000000u) | ((rem == 0x10000000u) & f);  // round to nearest even
         return __uint_as_float((hi & 0x80000000u) | f);
     }
-    return __double2float_rn(x);
+    return d2f_slow(x);
 }
 
 __device__ __forceinline__ double f2d_bits(float x) {
@@ -125,7 +133,7 @@ __device__ __forceinline__ double f2d_bits(float x) {
         return __hiloint2double(
             (int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3)),
             (int)(u << 29));
-    return (double)x;
+    return f2d_slow(x);
 }
 
 template <typename T>
