@@ -23,17 +23,102 @@
 
 #include "gclaw.h"
 #include "gclaw_step_impl.cuh"
+#include "gclaw_strip.cuh"
 
 namespace gclaw {
 
-// One problem of the device table (48 bytes).
+// One problem of the device table (48 bytes): its tile decomposition (tile
+// kernels) and its strip decomposition (FP32 strip kernels: strips of
+// STRIP_W columns times segments of BATCH_SEG rows).
 struct BatchEntry {
     int mx, my;
     int tiles_x, ntiles;
     double dx, dy;
     long long q_off;
-    long long pad;
+    int strips_x, nunits;
 };
+constexpr int BATCH_SEG = 64;
+
+// Batched FP32-bulk steps on warp strips: a persistent grid of warps strides
+// over the strip units (problem, strip, row segment) of all problems; a warp
+// finds the problem of its unit by probing the units' prefix sums forward
+// from the problem of its previous unit (its units only increase), marches
+// the unit exactly as the single-problem strip kernel does (so a problem's
+// result does not depend on being batched), reduces max |s| across its lanes
+// into the problem's control block, and the problem's last unit applies the
+// evolve_to_time rules.
+template <template <typename> class RPT>
+__global__ void __launch_bounds__(STRIP_NW * 32, StripCfg<RPT>::MINB)
+    batch_strip_kernel(const StepArgs base, const typename RPT<float>::Params P,
+                       const BatchEntry *__restrict__ ent, const int *__restrict__ ustart,
+                       int nprob, double *q0, double *q1, gclaw_ctrl *ctrls) {
+    constexpr bool RING = StripCfg<RPT>::RING;
+    extern __shared__ __align__(16) unsigned char strip_smem[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int nw = gridDim.x * STRIP_NW;
+    const int total = __ldg(ustart + nprob);
+    float *ring = RING ? reinterpret_cast<float *>(strip_smem) +
+                             wib * 32 * strip_ring_floats<RPT<float>>()
+                       : nullptr;
+    int pcur = 0;
+    for (int u = blockIdx.x * STRIP_NW + wib; u < total; u += nw) {
+        int lo = pcur;  // largest p with ustart[p] <= u
+        for (;;) {
+            const int idx = lo + 1 + lane;
+            const bool le = idx < nprob && __ldg(ustart + idx) <= u;
+            const int c = __popc(__ballot_sync(0xffffffffu, le));
+            lo += c;
+            if (c < 32) break;
+        }
+        pcur = lo;
+        gclaw_ctrl *c = ctrls + lo;
+        int done = 0, par = 0;
+        double dt = 0.0;
+        if (lane == 0) {
+            const volatile gclaw_ctrl *vc = c;
+            done = vc->done;
+            par = vc->parity;
+            dt = vc->dt;
+        }
+        done = __shfl_sync(0xffffffffu, done, 0);
+        if (done) continue;
+        par = __shfl_sync(0xffffffffu, par, 0);
+        dt = __shfl_sync(0xffffffffu, dt, 0);
+        const BatchEntry e = ent[lo];
+        StepArgs a = base;
+        a.mx = e.mx;
+        a.my = e.my;
+        a.dx = e.dx;
+        a.dy = e.dy;
+        double *qa = q0 + e.q_off, *qb = q1 + e.q_off;
+        const double *qin = par ? qb : qa;
+        double *qout = par ? qa : qb;
+        const int local = u - __ldg(ustart + lo);
+        const int strip = local % e.strips_x, seg = local / e.strips_x;
+        const int j0 = seg * BATCH_SEG, j1 = min(j0 + BATCH_SEG, e.my);
+        const double dtdx = dt / e.dx, dtdy = dt / e.dy;
+        float smax_x = 0.0f, smax_y = 0.0f;
+        bool bad = false;
+        strip_run<RPT, RING>(a, P, qin, qout, (float)dtdx, (float)dtdy, lane,
+                             strip * STRIP_W + lane - 2, j0, j1, smax_x, smax_y, bad, ring);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            smax_x = fmaxf(smax_x, __shfl_xor_sync(0xffffffffu, smax_x, off));
+            smax_y = fmaxf(smax_y, __shfl_xor_sync(0xffffffffu, smax_y, off));
+        }
+        const bool anybad = __any_sync(0xffffffffu, bad);
+        if (lane == 0) {
+            atomicMax(&c->smax_bits[0], (unsigned long long)__double_as_longlong((double)smax_x));
+            atomicMax(&c->smax_bits[1], (unsigned long long)__double_as_longlong((double)smax_y));
+            if (anybad) atomicOr(&c->flags, 1u);
+            __threadfence();
+            if (atomicAdd(&c->blocks_done, 1u) == (unsigned)e.nunits - 1u) {
+                __threadfence();
+                finish_step(c, 1, dt, dtdx, dtdy);
+            }
+        }
+    }
+}
 
 template <template <typename> class RPT, typename T, int TX, int TY, int NT>
 __global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1)
@@ -158,6 +243,38 @@ static int launch_batch(const gclaw_solver *s, const StepArgs &a, const void *ta
     return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
 }
 
+template <template <typename> class RPT>
+static int launch_batch_strip(const gclaw_solver *s, const StepArgs &a, const void *table,
+                              int nprob, double *q0, double *q1, gclaw_ctrl *ctrls, int nlaunch,
+                              cudaStream_t st) {
+    auto kern = batch_strip_kernel<RPT>;
+    constexpr size_t smem =
+        StripCfg<RPT>::RING ? sizeof(float) * STRIP_NW * 32 * strip_ring_floats<RPT<float>>() : 0;
+    static int grid_of_dev[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return GCLAW_ERR_CUDA;
+    if (grid_of_dev[dev] == 0) {
+        int sms = 0, per_sm = 0;
+        if ((smem > 48 * 1024 &&
+             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                 cudaSuccess) ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, STRIP_NW * 32, smem) !=
+                cudaSuccess ||
+            per_sm < 1)
+            return GCLAW_ERR_CUDA;
+        grid_of_dev[dev] = sms * per_sm;
+    }
+    const BatchEntry *ent = (const BatchEntry *)table;
+    const int *ustart = (const int *)((const char *)table + sizeof(BatchEntry) * (size_t)nprob +
+                                      sizeof(int) * ((size_t)nprob + 1));
+    const typename RPT<float>::Params P = RPT<float>::make(s->problem_data);
+    for (int l = 0; l < nlaunch; l++)
+        kern<<<grid_of_dev[dev], STRIP_NW * 32, smem, st>>>(a, P, ent, ustart, nprob, q0, q1,
+                                                            ctrls);
+    return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
+}
+
 // gclaw_check on the shared part of a batch's solver description (the
 // per-problem grid fields are ignored).
 static int check_shared(const gclaw_solver *s) {
@@ -176,7 +293,7 @@ extern "C" {
 
 size_t gclaw_batch_table_bytes(int nprob) {
     if (nprob < 1) return 0;
-    return sizeof(BatchEntry) * (size_t)nprob + sizeof(int) * ((size_t)nprob + 1);
+    return sizeof(BatchEntry) * (size_t)nprob + 2 * sizeof(int) * ((size_t)nprob + 1);
 }
 
 int gclaw_batch_prepare(const gclaw_solver *s, const gclaw_batch_problem *probs, int nprob,
@@ -193,7 +310,8 @@ int gclaw_batch_prepare(const gclaw_solver *s, const gclaw_batch_problem *probs,
     if (!host) return GCLAW_ERR_ARG;
     BatchEntry *ent = (BatchEntry *)host;
     int *tstart = (int *)(host + sizeof(BatchEntry) * (size_t)nprob);
-    long long tiles = 0;
+    int *ustart = tstart + nprob + 1;
+    long long tiles = 0, units = 0;
     for (int p = 0; p < nprob; p++) {
         const gclaw_batch_problem &b = probs[p];
         if (b.mx < 2 || b.my < 2 || !(b.dx > 0.0) || !(b.dy > 0.0) || b.q_offset < 0) {
@@ -207,15 +325,19 @@ int gclaw_batch_prepare(const gclaw_solver *s, const gclaw_batch_problem *probs,
         ent[p].dx = b.dx;
         ent[p].dy = b.dy;
         ent[p].q_off = b.q_offset;
-        ent[p].pad = 0;
+        ent[p].strips_x = (b.mx + STRIP_W - 1) / STRIP_W;
+        ent[p].nunits = ent[p].strips_x * ((b.my + BATCH_SEG - 1) / BATCH_SEG);
         tstart[p] = (int)tiles;
+        ustart[p] = (int)units;
         tiles += ent[p].ntiles;
-        if (tiles > 0x7fffffffll) {
+        units += ent[p].nunits;
+        if (tiles > 0x7fffffffll || units > 0x7fffffffll) {
             free(host);
             return GCLAW_ERR_ARG;
         }
     }
     tstart[nprob] = (int)tiles;
+    ustart[nprob] = (int)units;
     cudaStream_t st = (cudaStream_t)stream;
     const bool ok = cudaMemcpyAsync(table_dev, host, nbytes, cudaMemcpyHostToDevice, st) ==
                         cudaSuccess &&
@@ -257,6 +379,23 @@ int gclaw_batch_advance(const gclaw_solver *s, const void *table_dev, int nprob,
     a.tw = s->transverse_waves;
     cudaStream_t st = (cudaStream_t)stream;
     const bool f64 = s->precision == GCLAW_PREC_FP64;
+    // FP32-bulk runs on strips unless tiles were selected for the process
+    // (the same choice as for single problems, so batched and single runs
+    // of a problem agree bit for bit)
+    const int fam = gclaw_fp32_kernel(-1);
+    if (!f64 && fam != 1 && s->rp != GCLAW_RP_VC_ACOUSTICS_2D) {
+        switch (s->rp) {
+        case GCLAW_RP_ACOUSTICS_2D:
+            return launch_batch_strip<RpAcoustics>(s, a, table_dev, nprob, q0_dev, q1_dev,
+                                                   ctrls_dev, nlaunch, st);
+        case GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D:
+            return launch_batch_strip<RpShallow>(s, a, table_dev, nprob, q0_dev, q1_dev,
+                                                 ctrls_dev, nlaunch, st);
+        default:
+            return launch_batch_strip<RpEuler>(s, a, table_dev, nprob, q0_dev, q1_dev, ctrls_dev,
+                                               nlaunch, st);
+        }
+    }
 #define GCLAW_BATCH(RPT)                                                                         \
     (f64 ? launch_batch<RPT, double>(s, a, table_dev, nprob, total_tiles, q0_dev, q1_dev,       \
                                      ctrls_dev, nlaunch, st)                                     \

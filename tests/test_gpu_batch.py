@@ -1,11 +1,10 @@
 """Batched launch of independent problems against single-problem runs.
 
-Every problem of a batch runs the same tile body as a single problem on the
-tile kernel, so its state and its time-step control (t, dt, accepted and
-attempted steps) must equal those of the same problem advanced alone with
-the tile kernel, bit for bit -- including problems whose first dt is
-rejected.  (The FP32 default for single problems is the strip kernel,
-which agrees with the tile kernel to rounding.)"""
+Every problem of a batch runs the same body as a single problem (FP64: the
+tile kernel; FP32-bulk: the strip kernel, or tiles when selected for the
+process), so its state and its time-step control (t, dt, accepted and
+attempted steps) must equal those of the same problem advanced alone, bit
+for bit -- including problems whose first dt is rejected."""
 import math
 
 import numpy as np
@@ -42,9 +41,18 @@ def small_batch(nprob, seed, precision):
     return bs, shapes, deltas, qs, np.array(dt0)
 
 
-@pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_FP32_BULK])
-def test_batch_equals_single_problems(cuda, precision):
+@pytest.mark.parametrize("precision,family", [(_lib.PREC_FP64, 0), (_lib.PREC_FP32_BULK, 0),
+                                              (_lib.PREC_FP32_BULK, 1)])
+def test_batch_equals_single_problems(cuda, precision, family):
     nsteps = 12
+    prev = _lib.lib().gclaw_fp32_kernel(family)  # 0: default (strips), 1: tiles
+    try:
+        _batch_equals_single_problems(precision, nsteps)
+    finally:
+        _lib.lib().gclaw_fp32_kernel(prev)
+
+
+def _batch_equals_single_problems(precision, nsteps):
     bs, shapes, deltas, qs, dt0 = small_batch(24, 7 + precision, precision)
     bs.ctrl_init(dt0, max_accepted=nsteps, max_steps=100)
     for _ in range(4 * nsteps):
@@ -54,18 +62,14 @@ def test_batch_equals_single_problems(cuda, precision):
     assert np.all(ctrl["done"] == 1) and np.all(ctrl["status"] == 0)
     assert np.all(ctrl["numsteps"] == nsteps)
     assert np.any(ctrl["attempts"] > nsteps)  # the rejected first attempts
-    prev = _lib.lib().gclaw_fp32_kernel(1)  # single problems on the tile kernel too
-    try:
-        singles = []
-        for p, ((mx, my), (dx, dy)) in enumerate(zip(shapes, deltas)):
-            s = make_solver_struct(_lib.RP_SHALLOW_ROE_WITH_EFIX_2D, mx, my, dx, dy, [3, 1],
-                                   [1, 3], [4, 4, 4], 2, 2, precision, [1.0])
-            dev = DeviceProblem(s)
-            dev.upload(qs[p])
-            c = dev.evolve(0.0, dt0[p], math.inf, max_accepted=nsteps, max_steps=100)
-            singles.append((dev.download(c.parity), c))
-    finally:
-        _lib.lib().gclaw_fp32_kernel(prev)
+    singles = []
+    for p, ((mx, my), (dx, dy)) in enumerate(zip(shapes, deltas)):
+        s = make_solver_struct(_lib.RP_SHALLOW_ROE_WITH_EFIX_2D, mx, my, dx, dy, [3, 1],
+                               [1, 3], [4, 4, 4], 2, 2, precision, [1.0])
+        dev = DeviceProblem(s)
+        dev.upload(qs[p])
+        c = dev.evolve(0.0, dt0[p], math.inf, max_accepted=nsteps, max_steps=100)
+        singles.append((dev.download(c.parity), c))
     for p, (q1, c) in enumerate(singles):
         assert np.array_equal(q1, outs[p]), p
         assert (c.t, c.dt, c.numsteps, c.attempts) == (ctrl["t"][p], ctrl["dt"][p],

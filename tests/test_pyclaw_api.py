@@ -89,5 +89,5 @@ def test_batch_table_size():
     from clawpack_gb300 import _lib
 
     L = _lib.lib()
-    assert L.gclaw_batch_table_bytes(10) == 10 * 48 + 11 * 4
+    assert L.gclaw_batch_table_bytes(10) == 10 * 48 + 2 * 11 * 4  # entries, tile and strip starts
     assert L.gclaw_batch_table_bytes(0) == 0
