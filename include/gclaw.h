@@ -235,12 +235,14 @@ typedef struct gclaw_batch_problem {
     long long q_offset;  /* offset of the problem's state in the buffers (doubles) */
 } gclaw_batch_problem;
 
-/* Device bytes of the tile table for nprob problems. */
+/* Device bytes of the work table for nprob problems (per problem its tile
+ * and its strip decomposition, and the running starts of both). */
 size_t gclaw_batch_table_bytes(int nprob);
 
-/* Fill the tile table (caller-owned device memory, 16-byte aligned) for the
+/* Fill the work table (caller-owned device memory, 16-byte aligned) for the
  * problems described in host memory; returns the total number of tiles in
- * *total_tiles.  Synchronises the stream. */
+ * *total_tiles (the strip decomposition's size is kept in the table).
+ * Synchronises the stream. */
 int gclaw_batch_prepare(const gclaw_solver *s, const gclaw_batch_problem *probs, int nprob,
                         void *table_dev, size_t table_bytes, int *total_tiles, void *stream);
 
@@ -251,9 +253,11 @@ int gclaw_batch_ctrl_init(gclaw_ctrl *ctrls_dev, int nprob, const double *dt0_de
                           int max_steps, int max_accepted, int dt_variable, void *stream);
 
 /* Enqueue nlaunch batched steps (no synchronisation; capturable in a CUDA
- * graph).  Each launch is a persistent grid of resident CTAs striding over
- * all tiles of all problems; problem p's accepted state is in q0 or q1 per
- * ctrls_dev[p].parity. */
+ * graph).  Each launch is a persistent grid striding over all work units of
+ * all problems: tiles in FP64 (the tile body of gclaw_step), strips in
+ * FP32-bulk (the strip body, or tiles while gclaw_fp32_kernel(1) is in
+ * effect), so every problem evolves exactly as it would alone; problem p's
+ * accepted state is in q0 or q1 per ctrls_dev[p].parity. */
 int gclaw_batch_advance(const gclaw_solver *s, const void *table_dev, int nprob, int total_tiles,
                         double *q0_dev, double *q1_dev, gclaw_ctrl *ctrls_dev, int nlaunch,
                         void *stream);
