@@ -6,12 +6,15 @@
 // large FP64 buffers (q0, q1), problem p at offset q_offset[p], each in the
 // (num_eqn, mx, my) Fortran layout of a single problem.
 //
-// One launch of batch_step_kernel is one attempted step of every unfinished
-// problem: a persistent grid (resident CTAs only) strides over a table of
-// all tiles of all problems; a CTA finds the problem of its tile by binary
-// search over the tiles' prefix sums, runs the same tile body as the
-// single-problem kernel (so each problem's result is bit-identical to
-// stepping it alone), and feeds the problem's CFL reduction.  The last tile
+// One launch is one attempted step of every unfinished problem.  FP64
+// (batch_step_kernel): a persistent grid of CTAs strides over all tiles of
+// all problems; a CTA finds the problem of its tile by binary search over
+// the tiles' prefix sums and runs the single-problem tile body.  FP32-bulk
+// (batch_strip_kernel): a persistent grid of warps strides over all strip
+// units (problem, 28-column strip, 64-row segment) and runs the
+// single-problem strip body, which needs no barriers and suits small
+// problems.  Either way each problem's result is bit-identical to stepping
+// it alone, and each unit feeds the problem's CFL reduction.  The last unit
 // of a problem to finish applies PyClaw's evolve_to_time rules to that
 // problem's gclaw_ctrl (accept / reject, dt from its own CFL, stop after
 // max_accepted steps).  N steps are N launches, which capture into one CUDA
