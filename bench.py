@@ -502,7 +502,7 @@ def run_ours(args):
         q32 = dev32.q[c32.parity]
         err = float((q32 - q64).abs().sum() / q64.abs().sum())
         a32 = alg_bytes / (s32 / args.steps) * 1e-9
-        t32 = profiled("step_fp32_shallow", "dram_bytes_per_cell_update")
+        t32 = profiled("strip_fp32_shallow", "dram_bytes_per_cell_update")
         out["fp32_bulk"] = {"value": round(v32, 4), "unit": UNIT, "dtype": "f32 fluxes, f64 q",
                             "rel_l1_vs_fp64": err, "speedup_vs_fp64": round(v32 / value, 3),
                             "ms_per_step": round(s32 / args.steps * 1e3, 4),

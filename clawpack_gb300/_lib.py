@@ -119,6 +119,7 @@ SIGNATURES = {
     "gclaw_step2_noalloc": (_I, [_SP, _P, _P, _D, ctypes.POINTER(_D), _P]),
     "gclaw_adjoint_step": (_I, [_SP, _P, _P, _P, _D, _P]),
     "gclaw_fp32_kernel": (_I, [_I]),
+    "gclaw_fp64_kernel": (_I, [_I]),
     "gclaw_step_split": (_I, [_SP, _P, _P, _P, _D, _P, _P]),
     "gclaw_advance_split": (_I, [_SP, _P, _P, _P, _P, _I, _P]),
     "gclaw_batch_table_bytes": (_SZ, [_I]),

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(STRIP_NW * 32, StripCfg<RPT>::MINB)
     batch_strip_kernel(const StepArgs base, const typename RPT<float>::Params P,
                        const BatchEntry *__restrict__ ent, const int *__restrict__ ustart,
                        int nprob, double *q0, double *q1, gclaw_ctrl *ctrls) {
-    constexpr bool RING = StripCfg<RPT>::RING;
+    constexpr bool RING = strip_ring<RPT, float>();
     extern __shared__ __align__(16) unsigned char strip_smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int nw = gridDim.x * STRIP_NW;
@@ -102,8 +102,9 @@ __global__ void __launch_bounds__(STRIP_NW * 32, StripCfg<RPT>::MINB)
         const double dtdx = dt / e.dx, dtdy = dt / e.dy;
         float smax_x = 0.0f, smax_y = 0.0f;
         bool bad = false;
-        strip_run<RPT, RING>(a, P, qin, qout, (float)dtdx, (float)dtdy, lane,
-                             strip * STRIP_W + lane - 2, j0, j1, smax_x, smax_y, bad, ring);
+        strip_run<RPT, float, RING>(a, P, qin, qout, (float)dtdx, (float)dtdy, lane,
+                                    strip * STRIP_W + lane - 2, j0, j1, smax_x, smax_y, bad,
+                                    ring);
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
             smax_x = fmaxf(smax_x, __shfl_xor_sync(0xffffffffu, smax_x, off));
@@ -252,7 +253,8 @@ static int launch_batch_strip(const gclaw_solver *s, const StepArgs &a, const vo
                               cudaStream_t st) {
     auto kern = batch_strip_kernel<RPT>;
     constexpr size_t smem =
-        StripCfg<RPT>::RING ? sizeof(float) * STRIP_NW * 32 * strip_ring_floats<RPT<float>>() : 0;
+        strip_ring<RPT, float>() ? sizeof(float) * STRIP_NW * 32 * strip_ring_floats<RPT<float>>()
+                                 : 0;
     static int grid_of_dev[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return GCLAW_ERR_CUDA;

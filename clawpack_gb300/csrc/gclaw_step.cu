@@ -91,20 +91,20 @@ __global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1) step_kernel(const StepA
 // STRIP_W columns and seg_rows rows, units numbered strip-fastest so that
 // the warps of a block work on neighbouring strips of the same rows.
 #ifdef GCLAW_STRIP_MINB
-#define GCLAW_STRIP_BLOCKS(RPT) GCLAW_STRIP_MINB
+#define GCLAW_STRIP_BLOCKS(RPT, T) GCLAW_STRIP_MINB
 #else
-#define GCLAW_STRIP_BLOCKS(RPT) StripCfg<RPT>::MINB
+#define GCLAW_STRIP_BLOCKS(RPT, T) strip_minb<RPT, T>()
 #endif
-template <template <typename> class RPT>
-__global__ void __launch_bounds__(STRIP_NW * 32, GCLAW_STRIP_BLOCKS(RPT))
-    strip_kernel(const StepArgs a, const typename RPT<float>::Params P, int seg_rows, int nstrips,
+template <template <typename> class RPT, typename T>
+__global__ void __launch_bounds__(STRIP_NW * 32, GCLAW_STRIP_BLOCKS(RPT, T))
+    strip_kernel(const StepArgs a, const typename RPT<T>::Params P, int seg_rows, int nstrips,
                  int nunits) {
     constexpr int NT = STRIP_NW * 32;
-    constexpr bool RING = StripCfg<RPT>::RING;
+    constexpr bool RING = strip_ring<RPT, T>();
     extern __shared__ __align__(16) unsigned char strip_smem[];
     __shared__ double s_dt, s_dtdx, s_dtdy;
     __shared__ int s_par, s_skip;
-    __shared__ float s_red[2][STRIP_NW];
+    __shared__ T s_red[2][STRIP_NW];
 
     if (threadIdx.x == 0) {
         double dt;
@@ -128,21 +128,21 @@ __global__ void __launch_bounds__(STRIP_NW * 32, GCLAW_STRIP_BLOCKS(RPT))
     const double *__restrict__ qin = s_par ? a.qin[1] : a.qin[0];
     double *__restrict__ qout = s_par ? a.qout[1] : a.qout[0];
 
-    float smax_x = 0.0f, smax_y = 0.0f;
+    T smax_x = (T)0, smax_y = (T)0;
     bool bad = false;
     const int lane = threadIdx.x & 31;
     const int unit = blockIdx.x * STRIP_NW + (threadIdx.x >> 5);
     if (unit < nunits) {
         const int strip = unit % nstrips, seg = unit / nstrips;
         const int j0 = seg * seg_rows, j1 = min(j0 + seg_rows, a.my);
-        float *ring = RING ? reinterpret_cast<float *>(strip_smem) +
-                                 (threadIdx.x >> 5) * 32 * strip_ring_floats<RPT<float>>()
-                           : nullptr;
-        strip_run<RPT, RING>(a, P, qin, qout, (float)dtdx, (float)dtdy, lane,
-                             strip * STRIP_W + lane - 2, j0, j1, smax_x, smax_y, bad, ring);
+        T *ring = RING ? reinterpret_cast<T *>(strip_smem) +
+                             (threadIdx.x >> 5) * 32 * strip_ring_floats<RPT<T>>()
+                       : nullptr;
+        strip_run<RPT, T, RING>(a, P, qin, qout, (T)dtdx, (T)dtdy, lane,
+                                strip * STRIP_W + lane - 2, j0, j1, smax_x, smax_y, bad, ring);
     }
 
-    const int anybad = block_reduce<float, NT>(smax_x, smax_y, bad, s_red);
+    const int anybad = block_reduce<T, NT>(smax_x, smax_y, bad, s_red);
     if (threadIdx.x == 0) {
         gclaw_ctrl *c = a.ctrl;
         atomicMax(&c->smax_bits[0], (unsigned long long)__double_as_longlong((double)smax_x));
@@ -215,12 +215,14 @@ static int launch_tile(const gclaw_solver *s, const StepArgs &a, cudaStream_t st
 // 7.0 Gcell-updates/s); solvers that read transverse-neighbour aux run on
 // tiles.
 static int g_fp32_kernel = 0;
+// FP64 kernel family: 0 = default (tiles), 1 = tiles, 2 = strips.
+static int g_fp64_kernel = 0;
 
-template <template <typename> class RPT>
+template <template <typename> class RPT, typename T>
 static int launch_strip(const gclaw_solver *s, const StepArgs &a, cudaStream_t st, int nlaunch) {
-    auto kern = strip_kernel<RPT>;
+    auto kern = strip_kernel<RPT, T>;
     constexpr size_t smem =
-        StripCfg<RPT>::RING ? sizeof(float) * STRIP_NW * 32 * strip_ring_floats<RPT<float>>() : 0;
+        strip_ring<RPT, T>() ? sizeof(T) * STRIP_NW * 32 * strip_ring_floats<RPT<T>>() : 0;
     static int warp_slots[32] = {0};  // resident warps per GPU, per device ordinal < 32
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return GCLAW_ERR_CUDA;
@@ -248,7 +250,7 @@ static int launch_strip(const gclaw_solver *s, const StepArgs &a, cudaStream_t s
     nseg = (s->my + seg_rows - 1) / seg_rows;
     const int nunits = nstrips * nseg;
     const int nblocks = (nunits + STRIP_NW - 1) / STRIP_NW;
-    const typename RPT<float>::Params P = RPT<float>::make(s->problem_data);
+    const typename RPT<T>::Params P = RPT<T>::make(s->problem_data);
     for (int l = 0; l < nlaunch; l++)
         kern<<<nblocks, STRIP_NW * 32, smem, st>>>(a, P, seg_rows, nstrips, nunits);
     return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
@@ -268,9 +270,10 @@ static int launch_cfg(const gclaw_solver *s, const StepArgs &a, cudaStream_t st,
     using C = TileCfg<RPT, T>;
     if constexpr (!RPT<float>::TNB) {  // strips hold two rows only: no transverse-neighbour aux
         const bool split = a.sweeps == 1 || a.sweeps == 2;  // strips run both sweeps at once
-        if (sizeof(T) == 4 && !split &&
-            (g_fp32_kernel == 2 || (g_fp32_kernel == 0 && strip_default<RPT>())))
-            return launch_strip<RPT>(s, a, st, nlaunch);
+        const bool strips = sizeof(T) == 4 ? (g_fp32_kernel == 2 ||
+                                              (g_fp32_kernel == 0 && strip_default<RPT>()))
+                                           : g_fp64_kernel == 2;
+        if (strips && !split) return launch_strip<RPT, T>(s, a, st, nlaunch);
     }
     return launch_tile<RPT, T, C::TX, C::TY, C::NT>(s, a, st, nlaunch);
 }
@@ -436,6 +439,12 @@ int gclaw_step2(const gclaw_solver *s, const double *qold_dev, double *qnew_dev,
 int gclaw_fp32_kernel(int which) {
     const int prev = g_fp32_kernel;
     if (which >= 0 && which <= 2) g_fp32_kernel = which;
+    return prev;
+}
+
+int gclaw_fp64_kernel(int which) {
+    const int prev = g_fp64_kernel;
+    if (which >= 0 && which <= 2) g_fp64_kernel = which;
     return prev;
 }
 

@@ -47,23 +47,41 @@ constexpr int STRIP_MIN_ROWS = 16;
 // warp's shared memory (three slots rotating with the rows, lane-fastest,
 // each lane touching only its own column's slots) instead of registers, for
 // solvers whose records would not leave room for enough resident warps.
+// MINB64: the same for the FP64 kernel, which always uses the ring.
 template <template <typename> class RPT>
 struct StripCfg {
-    static constexpr int MINB = 3;
+    static constexpr int MINB = 3, MINB64 = 2;
     static constexpr bool RING = true;
 };
 template <>
 struct StripCfg<RpAcoustics> {
-    static constexpr int MINB = 4;
+    static constexpr int MINB = 4, MINB64 = 2;
     static constexpr bool RING = false;
 };
 template <>
 struct StripCfg<RpShallow> {
-    static constexpr int MINB = 4;  // 127 registers with the ring, no spills
+    static constexpr int MINB = 4, MINB64 = 2;  // FP32: 127 registers with the ring, no spills
     static constexpr bool RING = true;
 };
+template <template <typename> class RPT, typename T>
+__host__ __device__ constexpr bool strip_ring() {
+    return sizeof(T) == 8 || StripCfg<RPT>::RING;
+}
+template <template <typename> class RPT, typename T>
+__host__ __device__ constexpr int strip_minb() {
+    return sizeof(T) == 8 ? StripCfg<RPT>::MINB64 : StripCfg<RPT>::MINB;
+}
 
-// Floats of shared memory per lane for the y-edge ring of solver RP.
+// Real type of a solver instance RpX<T>.
+template <class RP>
+struct rp_real;
+template <template <typename> class R, typename T>
+struct rp_real<R<T>> {
+    using type = T;
+};
+
+// Elements (of the solver's real type) of shared memory per lane for the
+// y-edge ring of solver RP.
 template <class RP>
 __host__ __device__ constexpr int strip_ring_floats() {
     return 3 * (RP::MW * RP::M + RP::MW + 2 * RP::M + (RP::NR > 0 ? RP::NR : 1)) + 4 * RP::M;
@@ -79,17 +97,16 @@ __device__ __forceinline__ T shfl_dn1(T v) {
 }
 
 // Limiter, correction flux and transverse splitting of one edge (the body
-// of phase_limit for a single edge).  W is limited in place; wu_lo / wu_hi
-// are the waves of the edge below / above along the sweep (only the
-// components the solver can make nonzero are read).
-template <class RP, int IXY>
-__device__ __forceinline__ void strip_limit_edge(const typename RP::Params &P, float *W,
-                                                 const float *s, const float *wu_lo,
-                                                 const float *wu_hi, const float *am,
-                                                 const float *ap, const float *R, int mthlim,
-                                                 int order, int tw, float dtdn, float *fa,
-                                                 float *bmm, float *bpm, float *bmp, float *bpp) {
-    using T = float;
+// of phase_limit for a single edge, with the same expressions and tests).
+// W is limited in place; wu_lo / wu_hi are the waves of the edge below /
+// above along the sweep (only the components the solver can make nonzero
+// are read).
+template <class RP, int IXY, typename T>
+__device__ __forceinline__ void strip_limit_edge(const typename RP::Params &P, T *W, const T *s,
+                                                 const T *wu_lo, const T *wu_hi, const T *am,
+                                                 const T *ap, const T *R, int mthlim, int order,
+                                                 int tw, T dtdn, T *fa, T *bmm, T *bpm, T *bmp,
+                                                 T *bpp) {
     constexpr int M = RP::M, MW = RP::MW;
     T cq[M];
 #pragma unroll
@@ -103,9 +120,9 @@ __device__ __forceinline__ void strip_limit_edge(const typename RP::Params &P, f
 #pragma unroll
             for (int k = 0; k < M; k++)
                 if (RP::template wnz<IXY>(p, k)) wn2 = wn2 + W[p * M + k] * W[p * M + k];
-            if (wn2 == (T)0) continue;
+            if (eq0(wn2)) continue;
             T dot = (T)0;
-            if (s[p] > (T)0) {
+            if (gt0(s[p])) {
 #pragma unroll
                 for (int k = 0; k < M; k++)
                     if (RP::template wnz<IXY>(p, k)) dot = dot + wu_lo[p * M + k] * W[p * M + k];
@@ -114,7 +131,11 @@ __device__ __forceinline__ void strip_limit_edge(const typename RP::Params &P, f
                 for (int k = 0; k < M; k++)
                     if (RP::template wnz<IXY>(p, k)) dot = dot + W[p * M + k] * wu_hi[p * M + k];
             }
-            const T phi = (dot <= (T)0) ? (T)0 : philim<T>(lim, dot / wn2);
+            T phi = (T)0;
+            if (!le0(dot)) {
+                const T th = dot / wn2;
+                phi = gt0(th) ? philim_pos<T>(lim, th) : philim<T>(lim, th);
+            }
 #pragma unroll
             for (int k = 0; k < M; k++) W[p * M + k] = phi * W[p * M + k];
         }
@@ -125,7 +146,7 @@ __device__ __forceinline__ void strip_limit_edge(const typename RP::Params &P, f
 #pragma unroll
             for (int p = 0; p < MW; p++) {
                 if (!RP::template wnz<IXY>(p, k)) continue;
-                const T sa = fabsf(s[p]);
+                const T sa = (T)fabs(s[p]);
                 c = c + sa * ((T)1 - sa * dtave) * W[p * M + k];
             }
             cq[k] = c;
@@ -155,10 +176,11 @@ __device__ __forceinline__ void strip_limit_edge(const typename RP::Params &P, f
     }
 }
 
-// One y-edge record kept in registers between rows.
+// One y-edge record between rows.
 template <class RP>
 struct StripEdge {
-    float W[RP::MW * RP::M], s[RP::MW], am[RP::M], ap[RP::M], R[RP::NR > 0 ? RP::NR : 1];
+    using T = typename rp_real<RP>::type;
+    T W[RP::MW * RP::M], s[RP::MW], am[RP::M], ap[RP::M], R[RP::NR > 0 ? RP::NR : 1];
 };
 
 template <class RP>
@@ -171,11 +193,12 @@ __device__ __forceinline__ void load_row(const StepArgs &a, const double *__rest
 // y-edge records in a warp's shared-memory ring: slot-major, field, lane.
 template <class RP>
 struct StripRing {
+    using T = typename rp_real<RP>::type;
     static constexpr int NW = RP::MW * RP::M, NR = RP::NR > 0 ? RP::NR : 1;
     static constexpr int NF = NW + RP::MW + 2 * RP::M + NR;
-    float *base;  // this warp's area, lane-offset applied
-    __device__ __forceinline__ float &at(int slot, int f) const { return base[(slot * NF + f) * 32]; }
-    __device__ __forceinline__ float &lim(int f) const { return base[(3 * NF + f) * 32]; }
+    T *base;  // this warp's area, lane-offset applied
+    __device__ __forceinline__ T &at(int slot, int f) const { return base[(slot * NF + f) * 32]; }
+    __device__ __forceinline__ T &lim(int f) const { return base[(3 * NF + f) * 32]; }
     __device__ __forceinline__ void put(int slot, const StripEdge<RP> &e) const {
 #pragma unroll
         for (int f = 0; f < NW; f++)
@@ -193,7 +216,7 @@ struct StripRing {
     __device__ __forceinline__ void get(int slot, StripEdge<RP> &e) const {
 #pragma unroll
         for (int f = 0; f < NW; f++)
-            e.W[f] = RP::template wnz<2>(f / RP::M, f % RP::M) ? at(slot, f) : 0.0f;
+            e.W[f] = RP::template wnz<2>(f / RP::M, f % RP::M) ? at(slot, f) : (T)0;
 #pragma unroll
         for (int p = 0; p < RP::MW; p++) e.s[p] = at(slot, NW + p);
 #pragma unroll
@@ -204,23 +227,27 @@ struct StripRing {
 #pragma unroll
         for (int r = 0; r < NR; r++) e.R[r] = at(slot, NW + RP::MW + 2 * RP::M + r);
     }
-    __device__ __forceinline__ void get_w(int slot, float *W) const {
+    __device__ __forceinline__ void get_w(int slot, T *W) const {
 #pragma unroll
         for (int f = 0; f < NW; f++)
-            W[f] = RP::template wnz<2>(f / RP::M, f % RP::M) ? at(slot, f) : 0.0f;
+            W[f] = RP::template wnz<2>(f / RP::M, f % RP::M) ? at(slot, f) : (T)0;
     }
 };
 
-// The march of one warp over rows [j0, j1) of its strip.  ring: this warp's
-// shared-memory area (strip_ring_floats per lane) when RING.
-template <template <typename> class RPT, bool RING>
-__device__ __forceinline__ void strip_run(const StepArgs &a, const typename RPT<float>::Params &P,
+// The march of one warp over rows [j0, j1) of its strip.  T is the
+// arithmetic type: float for FP32-bulk (the window holds increments added to
+// the FP64 state at the end), double for FP64 (the window holds the state
+// itself, each row starting from q in the tile kernel's order, so the
+// -fmad=false build reproduces the oracle).  ring: this warp's shared-memory
+// area (strip_ring_floats elements of T per lane) when RING.
+template <template <typename> class RPT, typename T, bool RING>
+__device__ __forceinline__ void strip_run(const StepArgs &a, const typename RPT<T>::Params &P,
                                           const double *__restrict__ qin,
-                                          double *__restrict__ qout, float dtdx, float dtdy,
-                                          int lane, int c, int j0, int j1, float &smax_x,
-                                          float &smax_y, bool &bad, float *ring) {
-    using RP = RPT<float>;
-    using T = float;
+                                          double *__restrict__ qout, T dtdx, T dtdy, int lane,
+                                          int c, int j0, int j1, T &smax_x, T &smax_y, bool &bad,
+                                          T *ring) {
+    using RP = RPT<T>;
+    constexpr bool F64 = sizeof(T) == 8;
     const StripRing<RP> yr{ring + lane};
     int so = 0, sm = 1, sn = 2;  // ring slots of the y-edges r-5/2, r-3/2, r-1/2
     constexpr int M = RP::M, MW = RP::MW, NR = RP::NR > 0 ? RP::NR : 1;
@@ -242,7 +269,7 @@ __device__ __forceinline__ void strip_run(const StepArgs &a, const typename RPT<
     T qp[M], ap_[NA];   // row r-1 and its aux
     T qc[M], ac[NA];    // row r
     StripEdge<RP> Eo, Em;  // y-edges r-5/2 (W, s used) and r-3/2
-    T A0[M], A1[M], A2[M], A3[M];  // increments of rows r-2 .. r+1
+    T A0[M], A1[M], A2[M], A3[M];  // rows r-2 .. r+1 (increments, or states in FP64)
     T LAP[M], LFA[M], LBMP[M], LBPP[M];  // limited y-edge j-1/2 of the output row j
 #pragma unroll
     for (int k = 0; k < M; k++) A0[k] = A1[k] = A2[k] = A3[k] = (T)0;
@@ -253,12 +280,22 @@ __device__ __forceinline__ void strip_run(const StepArgs &a, const typename RPT<
     Em = StripEdge<RP>{};
     Eo = Em;
 
-    double qn[M];
+    // FP32: row r+1 is loaded during row r.  FP64: rows are loaded two ahead,
+    // because the accumulator of row r+2 starts from its state at the end of
+    // row r.
+    double qn[M], qf[M];
     load_row<RP>(a, qin, c, j0 - 2, qn);
+    if constexpr (F64) load_row<RP>(a, qin, c, j0 - 1, qf);
     for (int r = j0 - 2; r <= j1 + 1; r++) {
 #pragma unroll
         for (int k = 0; k < M; k++) qc[k] = from_double<T>(qn[k]);
-        if (r <= j1) load_row<RP>(a, qin, c, r + 1, qn);  // in flight during this row
+        if constexpr (F64) {
+#pragma unroll
+            for (int k = 0; k < M; k++) qn[k] = qf[k];
+            if (r + 2 <= j1 + 1) load_row<RP>(a, qin, c, r + 2, qf);  // in flight
+        } else {
+            if (r <= j1) load_row<RP>(a, qin, c, r + 1, qn);  // in flight during this row
+        }
         RP::cell_aux(P, qc, ac);
 
         // ---- x-sweep of row r -------------------------------------------------
@@ -275,8 +312,8 @@ __device__ __forceinline__ void strip_run(const StepArgs &a, const typename RPT<
                 bad |= eb;
 #pragma unroll
                 for (int p = 0; p < MW; p++) {
-                    bad |= (s[p] != s[p]);
-                    smax_x = tmax(smax_x, fabsf(s[p]));
+                    bad |= isnan_v(s[p]);
+                    smax_x = max_abs(smax_x, s[p]);
                 }
             }
             // upwind waves of the neighbouring edges (lanes L-1, L+1)
@@ -318,8 +355,8 @@ __device__ __forceinline__ void strip_run(const StepArgs &a, const typename RPT<
                 bad |= eb;
 #pragma unroll
                 for (int p = 0; p < MW; p++) {
-                    bad |= (En.s[p] != En.s[p]);
-                    smax_y = tmax(smax_y, fabsf(En.s[p]));
+                    bad |= isnan_v(En.s[p]);
+                    smax_y = max_abs(smax_y, En.s[p]);
                 }
             }
             if (r >= j0 + 1) {
@@ -365,8 +402,10 @@ __device__ __forceinline__ void strip_run(const StepArgs &a, const typename RPT<
                         const size_t o =
                             (size_t)M * ((size_t)(c + ooff) + (size_t)onx * (size_t)(j + ooff));
 #pragma unroll
-                        for (int k = 0; k < M; k++)
-                            qout[o + k] = __ldg(qin + o + k) + f2d_bits(A0[k]);
+                        for (int k = 0; k < M; k++) {
+                            if constexpr (F64) qout[o + k] = (double)A0[k];
+                            else qout[o + k] = __ldg(qin + o + k) + f2d_bits((float)A0[k]);
+                        }
                     }
                 }
 #pragma unroll
@@ -402,7 +441,7 @@ __device__ __forceinline__ void strip_run(const StepArgs &a, const typename RPT<
             A0[k] = A1[k];
             A1[k] = A2[k];
             A2[k] = A3[k];
-            A3[k] = (T)0;
+            A3[k] = F64 ? (T)qf[k] : (T)0;  // FP64: row r+2 starts from its state
         }
 #pragma unroll
         for (int f = 0; f < NA; f++) ap_[f] = ac[f];

@@ -42,6 +42,7 @@ def main(argv=None):
     p.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     p.add_argument("--adjoint", action="store_true")
     p.add_argument("--fp32-kernel", default="auto", choices=["auto", "tile", "strip"])
+    p.add_argument("--fp64-kernel", default="auto", choices=["auto", "tile", "strip"])
     p.add_argument("--split", action="store_true", help="dimensionally split steps")
     p.add_argument("--batched", type=int, default=0,
                    help="time the first N problems of the seeded shallow-water ensemble")
@@ -49,6 +50,7 @@ def main(argv=None):
     from . import _lib
 
     _lib.lib().gclaw_fp32_kernel({"auto": 0, "tile": 1, "strip": 2}[a.fp32_kernel])
+    _lib.lib().gclaw_fp64_kernel({"auto": 0, "tile": 1, "strip": 2}[a.fp64_kernel])
     if a.batched:
         return run_batched(a)
     w = make_workload(a.workload, a.mx, a.my or a.mx)

@@ -145,6 +145,10 @@ int gclaw_ctrl_init(gclaw_ctrl *ctrl_dev, double t, double dt, double t_end, dou
  * step; any other value only queries.  Returns the previous setting. */
 int gclaw_fp32_kernel(int which);
 
+/* The same for the FP64 step: 0 = default (tiles), 1 = tiles, 2 = register
+ * strips (bit-identical to tiles with -fmad=false). */
+int gclaw_fp64_kernel(int which);
+
 /* Drop-in for classic2.step2 (upstream pyclaw/src/pyclaw/classic/step2.f90):
  * one unsplit step of a ghost-filled qbc.  qold_dev and qnew_dev are
  * (num_eqn, mx+4, my+4) Fortran order; the interior of qnew_dev receives the
