@@ -21,6 +21,7 @@ RP_ACOUSTICS_2D = 1
 RP_SHALLOW_ROE_WITH_EFIX_2D = 2
 RP_EULER_4WAVE_2D = 3
 RP_VC_ACOUSTICS_2D = 4
+RP_SHALLOW_BATHYMETRY_FWAVE_2D = 5
 
 PREC_FP64 = 0
 PREC_FP32_BULK = 1

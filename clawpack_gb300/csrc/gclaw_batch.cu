@@ -388,7 +388,8 @@ int gclaw_batch_advance(const gclaw_solver *s, const void *table_dev, int nprob,
     // (the same choice as for single problems, so batched and single runs
     // of a problem agree bit for bit)
     const int fam = gclaw_fp32_kernel(-1);
-    if (!f64 && fam != 1 && s->rp != GCLAW_RP_VC_ACOUSTICS_2D) {
+    if (rp_user_aux(s->rp)) return GCLAW_ERR_UNSUPPORTED;  // no per-problem aux
+    if (!f64 && fam != 1) {
         switch (s->rp) {
         case GCLAW_RP_ACOUSTICS_2D:
             return launch_batch_strip<RpAcoustics>(s, a, table_dev, nprob, q0_dev, q1_dev,
@@ -407,7 +408,6 @@ int gclaw_batch_advance(const gclaw_solver *s, const void *table_dev, int nprob,
          : launch_batch<RPT, float>(s, a, table_dev, nprob, total_tiles, q0_dev, q1_dev,        \
                                     ctrls_dev, nlaunch, st))
     switch (s->rp) {
-    case GCLAW_RP_VC_ACOUSTICS_2D: return GCLAW_ERR_UNSUPPORTED;  // no per-problem aux
     case GCLAW_RP_ACOUSTICS_2D: return GCLAW_BATCH(RpAcoustics);
     case GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D: return GCLAW_BATCH(RpShallow);
     default: return GCLAW_BATCH(RpEuler);

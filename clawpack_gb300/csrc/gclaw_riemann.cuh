@@ -127,6 +127,19 @@ __device__ __forceinline__ double max_abs<double>(double m, double s) {
     return a <= F64_INF_BITS && a > b ? __longlong_as_double(a) : m;
 }
 
+// copysign(1, s) * x, exactly, as a sign-bit exchange on the integer pipes.
+template <typename T>
+__device__ __forceinline__ T sign_times(T x, T s);
+template <>
+__device__ __forceinline__ double sign_times<double>(double x, double s) {
+    return __longlong_as_double(__double_as_longlong(x) ^
+                                (__double_as_longlong(s) & (long long)0x8000000000000000ull));
+}
+template <>
+__device__ __forceinline__ float sign_times<float>(float x, float s) {
+    return __int_as_float(__float_as_int(x) ^ (__float_as_int(s) & (int)0x80000000u));
+}
+
 // True when fl(m / h - sqrt(g h)) > 0 cannot hold, decided without the
 // division and the square root: h > 0 and either m <= 0 (the quotient is
 // not positive) or m^2 < 0.81 g h^3 (|m / h| < 0.9 sqrt(g h) exactly, a
@@ -151,6 +164,7 @@ template <typename T>
 struct RpAcoustics {
     static constexpr int M = 3, MW = 2, NR = 0, NA = 0, NUA = 0;
     static constexpr bool TNB = false;  // rpn2 does not read the transverse neighbours
+    static constexpr bool FWAVE = false;
     struct Params {
         T cc, zz;
     };
@@ -209,7 +223,7 @@ struct RpAcoustics {
 template <typename T>
 struct RpVcAcoustics {
     static constexpr int M = 3, MW = 2, NR = 10, NA = 2, NUA = 2;
-    static constexpr bool TNB = true;
+    static constexpr bool TNB = true, FWAVE = false;
     struct Params {
         int unused;
     };
@@ -287,7 +301,7 @@ __device__ __forceinline__ void split_sum(const T *sb, const T *wb, T *bm, T *bp
 template <typename T>
 struct RpShallow {
     static constexpr int M = 3, MW = 3, NR = 4, NA = 6, NUA = 0;
-    static constexpr bool TNB = false;
+    static constexpr bool TNB = false, FWAVE = false;
     struct Params {
         T g;
         double gd;
@@ -470,6 +484,107 @@ struct RpShallow {
 };
 
 // ---------------------------------------------------------------------------
+// Shallow water over bathymetry, f-wave form: q = (h, hu, hv), user aux (b).
+// The flux difference plus the bathymetry source, delta = f(qr) - f(ql) +
+// (0, g hbar (br - bl), 0), is split into f-waves along the eigenvectors of
+// the Roe matrix (Bale, LeVeque, Mitran and Rossmanith, SIAM J. Sci. Comput.
+// 24 (2002); upstream riemann rpn2_shallow_bathymetry_fwave.f90); the
+// fluctuations are the f-waves of negative / positive speed, half each at
+// speed zero.  A lake at rest (h + b constant, no velocity) gives delta = 0.
+// Roe averages and the transverse split are those of RpShallow.
+// aux = (b, sqrt h, hu / sqrt h, hv / sqrt h, hu / h, hv / h).
+// ---------------------------------------------------------------------------
+template <typename T>
+struct RpShallowFwave {
+    static constexpr int M = 3, MW = 3, NR = 4, NA = 6, NUA = 1;
+    static constexpr bool TNB = false, FWAVE = true;
+    using Params = typename RpShallow<T>::Params;
+    static Params make(const double *pd) { return RpShallow<T>::make(pd); }
+
+    template <int IXY>
+    __host__ __device__ static constexpr bool wnz(int p, int k) {
+        return RpShallow<T>::template wnz<IXY>(p, k);
+    }
+
+    // aux[0] holds b on entry and keeps it; the depth terms follow
+    __device__ __forceinline__ static void cell_aux_user(const Params &P, const T *q, T *aux) {
+        T a6[6];
+        RpShallow<T>::cell_aux(P, q, a6);
+#pragma unroll
+        for (int f = 0; f < 5; f++) aux[1 + f] = a6[f];
+    }
+
+    template <int IXY>
+    __device__ __forceinline__ static bool rpn2(const Params &P, const T *ql, const T *qr,
+                                                const T *al, const T *ar, T *Z, T *s, T *am,
+                                                T *ap, T *R) {
+        constexpr int mu = IXY, mv = 3 - IXY;
+        const T g = P.g;
+        const T hl = ql[0], hr = qr[0];
+        if (!gt0(hl) || !gt0(hr)) {
+#pragma unroll
+            for (int f = 0; f < 9; f++) Z[f] = (T)0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                s[k] = am[k] = ap[k] = (T)0;
+                R[k] = (T)0;
+            }
+            R[3] = (T)0;
+            return true;
+        }
+        RpShallow<T>::template roe<IXY>(P, ql, qr, al + 1, ar + 1, R);
+        const T ubar = R[0], vbar = R[1], cbar = R[2];
+        const T ul = al[3 + mu], vl = al[3 + mv], ur = ar[3 + mu], vr = ar[3 + mv];
+        const T hbar = (hl + hr) * (T)0.5;
+        const T d0 = qr[mu] - ql[mu];
+        const T d1 = (qr[mu] * ur + (T)0.5 * g * hr * hr) - (ql[mu] * ul + (T)0.5 * g * hl * hl) +
+                     g * hbar * (ar[0] - al[0]);
+        const T d2 = qr[mu] * vr - ql[mu] * vl;
+        s[0] = ubar - cbar;
+        s[1] = ubar;
+        s[2] = ubar + cbar;
+#ifdef GCLAW_STRICT
+        const T b1 = (s[2] * d0 - d1) / (s[2] - s[0]);
+        const T b3 = (d1 - s[0] * d0) / (s[2] - s[0]);
+#else
+        const T rd = (T)1 / (s[2] - s[0]);
+        const T b1 = (s[2] * d0 - d1) * rd;
+        const T b3 = (d1 - s[0] * d0) * rd;
+#endif
+        const T b2 = d2 - vbar * d0;
+        T *z1 = Z, *z2 = Z + 3, *z3 = Z + 6;
+        z1[0] = b1; z1[mu] = b1 * s[0]; z1[mv] = b1 * vbar;
+        z2[0] = (T)0; z2[mu] = (T)0; z2[mv] = b2;
+        z3[0] = b3; z3[mu] = b3 * s[2]; z3[mv] = b3 * vbar;
+#pragma unroll
+        for (int k = 0; k < 3; k++) am[k] = ap[k] = (T)0;
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+            const bool neg = lt0(s[p]), pos = gt0(s[p]);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const T z = Z[3 * p + k];
+                if (neg) {
+                    am[k] = am[k] + z;
+                } else if (pos) {
+                    ap[k] = ap[k] + z;
+                } else {
+                    am[k] = am[k] + (T)0.5 * z;
+                    ap[k] = ap[k] + (T)0.5 * z;
+                }
+            }
+        }
+        return false;
+    }
+
+    template <int IXY>
+    __device__ __forceinline__ static void rpt2(const Params &P, const T *R, const T *asdq, T *bm,
+                                                T *bp) {
+        RpShallow<T>::template rpt2<IXY>(P, R, asdq, bm, bp);
+    }
+};
+
+// ---------------------------------------------------------------------------
 // 2D Euler, Roe solver with 4 waves (acoustic u-c, entropy u, shear u,
 // acoustic u+c) and optional Harten-Hyman entropy fix: q = (rho, rhou, rhov, E).
 // Roe state kept for rpt2: R = (u, v, enth, u2v2, a, g1a2, euv).
@@ -477,7 +592,7 @@ struct RpShallow {
 template <typename T>
 struct RpEuler {
     static constexpr int M = 4, MW = 4, NR = 7, NA = 8, NUA = 0;
-    static constexpr bool TNB = false;
+    static constexpr bool TNB = false, FWAVE = false;
     struct Params {
         T gamma, gamma1;
         int efix;

@@ -268,7 +268,8 @@ bool strip_default<RpEuler>() { return true; }
 template <template <typename> class RPT, typename T>
 static int launch_cfg(const gclaw_solver *s, const StepArgs &a, cudaStream_t st, int nlaunch) {
     using C = TileCfg<RPT, T>;
-    if constexpr (!RPT<float>::TNB) {  // strips hold two rows only: no transverse-neighbour aux
+    // strips hold two rows of q only: no user aux, no transverse-neighbour aux
+    if constexpr (!RPT<float>::TNB && RPT<float>::NUA == 0) {
         const bool split = a.sweeps == 1 || a.sweeps == 2;  // strips run both sweeps at once
         const bool strips = sizeof(T) == 4 ? (g_fp32_kernel == 2 ||
                                               (g_fp32_kernel == 0 && strip_default<RPT>()))
@@ -293,6 +294,9 @@ static int dispatch(const gclaw_solver *s, const StepArgs &a, cudaStream_t st, i
     case GCLAW_RP_VC_ACOUSTICS_2D:
         return f64 ? launch_cfg<RpVcAcoustics, double>(s, a, st, nlaunch)
                    : launch_cfg<RpVcAcoustics, float>(s, a, st, nlaunch);
+    case GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D:
+        return f64 ? launch_cfg<RpShallowFwave, double>(s, a, st, nlaunch)
+                   : launch_cfg<RpShallowFwave, float>(s, a, st, nlaunch);
     default: return GCLAW_ERR_ARG;
     }
 }
@@ -310,7 +314,7 @@ static void fill_args(const gclaw_solver *s, StepArgs &a) {
     for (int p = 0; p < 4; p++) a.mthlim |= (s->mthlim[p] & 0xff) << (8 * p);
     a.order = s->order;
     a.tw = s->transverse_waves;
-    a.aux = s->rp == GCLAW_RP_VC_ACOUSTICS_2D ? s->aux : nullptr;
+    a.aux = rp_user_aux(s->rp) ? s->aux : nullptr;
     for (int d = 0; d < 2; d++) {
         a.abc_lo[d] = s->aux_bc_lower[d];
         a.abc_hi[d] = s->aux_bc_upper[d];
@@ -348,6 +352,7 @@ int gclaw_rp_shape(int rp, int *num_eqn, int *num_waves) {
     case GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D: *num_eqn = 3; *num_waves = 3; return GCLAW_OK;
     case GCLAW_RP_EULER_4WAVE_2D: *num_eqn = 4; *num_waves = 4; return GCLAW_OK;
     case GCLAW_RP_VC_ACOUSTICS_2D: *num_eqn = 3; *num_waves = 2; return GCLAW_OK;
+    case GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D: *num_eqn = 3; *num_waves = 3; return GCLAW_OK;
     default: return GCLAW_ERR_ARG;
     }
 }
@@ -381,6 +386,8 @@ int gclaw_check(const gclaw_solver *s) {
         if (!(pd[0] > 0.0)) return GCLAW_ERR_ARG;
         break;
     case GCLAW_RP_VC_ACOUSTICS_2D:
+    case GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D:
+        if (s->rp == GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D && !(pd[0] > 0.0)) return GCLAW_ERR_ARG;
         if (!s->aux) return GCLAW_ERR_ARG;
         for (int d = 0; d < 2; d++) {
             if (s->aux_bc_lower[d] < GCLAW_BC_EXTRAP || s->aux_bc_lower[d] > GCLAW_BC_WALL ||
@@ -509,7 +516,7 @@ int gclaw_step_split(const gclaw_solver *s, const double *q_dev, double *qnew_de
     int rc = gclaw_check(s);
     if (rc) return rc;
     if (!q_dev || !qnew_dev || !qtmp_dev || !ws_dev || !(dt > 0.0)) return GCLAW_ERR_ARG;
-    if (s->rp == GCLAW_RP_VC_ACOUSTICS_2D) return GCLAW_ERR_UNSUPPORTED;
+    if (rp_user_aux(s->rp)) return GCLAW_ERR_UNSUPPORTED;
     if (qtmp_dev == q_dev || qtmp_dev == qnew_dev || q_dev == qnew_dev) return GCLAW_ERR_ARG;
     StepArgs a{};
     fill_args(s, a);
@@ -527,7 +534,7 @@ int gclaw_advance_split(const gclaw_solver *s, double *q0_dev, double *q1_dev, d
     int rc = gclaw_check(s);
     if (rc) return rc;
     if (!q0_dev || !q1_dev || !qtmp_dev || !ctrl_dev || nsteps < 0) return GCLAW_ERR_ARG;
-    if (s->rp == GCLAW_RP_VC_ACOUSTICS_2D) return GCLAW_ERR_UNSUPPORTED;
+    if (rp_user_aux(s->rp)) return GCLAW_ERR_UNSUPPORTED;
     if (qtmp_dev == q0_dev || qtmp_dev == q1_dev || q0_dev == q1_dev) return GCLAW_ERR_ARG;
     StepArgs a{};
     fill_args(s, a);
@@ -802,6 +809,7 @@ extern "C" int gclaw_step2_noalloc(const gclaw_solver *s, const double *qold_dev
     case GCLAW_RP_ACOUSTICS_2D: rc = GCLAW_LAUNCH_NA(RpAcoustics); break;
     case GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D: rc = GCLAW_LAUNCH_NA(RpShallow); break;
     case GCLAW_RP_VC_ACOUSTICS_2D: rc = GCLAW_LAUNCH_NA(RpVcAcoustics); break;
+    case GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D: rc = GCLAW_LAUNCH_NA(RpShallowFwave); break;
     default: rc = GCLAW_LAUNCH_NA(RpEuler); break;
     }
 #undef GCLAW_LAUNCH_NA

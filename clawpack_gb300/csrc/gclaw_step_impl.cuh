@@ -99,6 +99,11 @@ __device__ __forceinline__ double load_a(const StepArgs &a, int k, int gi, int g
     return __ldg(a.aux + k + (size_t)NUA * ((size_t)si + (size_t)a.mx * (size_t)sj));
 }
 
+// Solvers that read a user aux array (gclaw_solver.aux).
+inline bool rp_user_aux(int rp) {
+    return rp == GCLAW_RP_VC_ACOUSTICS_2D || rp == GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D;
+}
+
 // Exact double <-> float conversions done with integer operations.  On
 // GB300 the conversion instructions issue to the FP64 pipe, which is the
 // scarce unit; these give the same bits as __double2float_rn and the float
@@ -190,7 +195,9 @@ GCLAW_TILE_CFG(RpAcoustics, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_
 GCLAW_TILE_CFG(RpShallow, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_TILE_F64_NT)
 GCLAW_TILE_CFG(RpEuler, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_TILE_F64_NT)
 GCLAW_TILE_CFG(RpVcAcoustics, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_TILE_F64_NT)
+GCLAW_TILE_CFG(RpShallowFwave, double, GCLAW_TILE_F64_TX, GCLAW_TILE_F64_TY, GCLAW_TILE_F64_NT)
 #else
+GCLAW_TILE_CFG(RpShallowFwave, double, 32, 16, 256)
 GCLAW_TILE_CFG(RpVcAcoustics, double, 32, 16, 256)
 GCLAW_TILE_CFG(RpAcoustics, double, 32, 16, 256)
 GCLAW_TILE_CFG(RpShallow, double, 32, 16, 256)
@@ -201,7 +208,9 @@ GCLAW_TILE_CFG(RpAcoustics, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_T
 GCLAW_TILE_CFG(RpShallow, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_TILE_F32_NT)
 GCLAW_TILE_CFG(RpEuler, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_TILE_F32_NT)
 GCLAW_TILE_CFG(RpVcAcoustics, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_TILE_F32_NT)
+GCLAW_TILE_CFG(RpShallowFwave, float, GCLAW_TILE_F32_TX, GCLAW_TILE_F32_TY, GCLAW_TILE_F32_NT)
 #else
+GCLAW_TILE_CFG(RpShallowFwave, float, 32, 16, 512)
 GCLAW_TILE_CFG(RpVcAcoustics, float, 32, 16, 512)
 GCLAW_TILE_CFG(RpAcoustics, float, 32, 16, 512)
 GCLAW_TILE_CFG(RpShallow, float, 32, 16, 512)
@@ -224,6 +233,10 @@ static inline void tile_shape(int rp, int precision, int *tx, int *ty) {
     case GCLAW_RP_VC_ACOUSTICS_2D:
         *tx = f64 ? TileCfg<RpVcAcoustics, double>::TX : TileCfg<RpVcAcoustics, float>::TX;
         *ty = f64 ? TileCfg<RpVcAcoustics, double>::TY : TileCfg<RpVcAcoustics, float>::TY;
+        return;
+    case GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D:
+        *tx = f64 ? TileCfg<RpShallowFwave, double>::TX : TileCfg<RpShallowFwave, float>::TX;
+        *ty = f64 ? TileCfg<RpShallowFwave, double>::TY : TileCfg<RpShallowFwave, float>::TY;
         return;
     default:
         *tx = f64 ? TileCfg<RpEuler, double>::TX : TileCfg<RpEuler, float>::TX;
@@ -294,7 +307,7 @@ struct Tile {
 // ---- phase 0: per-cell square roots and quotients for one sweep ---------
 template <class RP, typename T, int IXY, int TX, int TY, int NT>
 __device__ __forceinline__ void phase_aux(const typename RP::Params &P, const T *QS, T *CA) {
-    static_assert(RP::NUA == 0 || RP::NUA == RP::NA, "user aux is transformed in the aux area");
+    static_assert(RP::NUA <= RP::NA, "user aux is the first planes of the aux area");
     using TL = Tile<RP, TX, TY>;
     constexpr int M = RP::M, NA = RP::NA;
     if (NA == 0) return;
@@ -460,7 +473,10 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
                 for (int p = 0; p < MW; p++) {
                     if (!RP::template wnz<IXY>(p, k)) continue;
                     const T sa = fabs(s[p]);
-                    c = c + sa * ((T)1 - sa * dtave) * W[p * M + k];
+                    if constexpr (RP::FWAVE)  // sign(s) (1 - |s| dt/dx) Z
+                        c = c + sign_times((T)1 - sa * dtave, s[p]) * W[p * M + k];
+                    else
+                        c = c + sa * ((T)1 - sa * dtave) * W[p * M + k];
                 }
                 cq[k] = c;
             }

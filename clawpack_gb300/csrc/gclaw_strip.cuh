@@ -147,7 +147,10 @@ __device__ __forceinline__ void strip_limit_edge(const typename RP::Params &P, T
             for (int p = 0; p < MW; p++) {
                 if (!RP::template wnz<IXY>(p, k)) continue;
                 const T sa = (T)fabs(s[p]);
-                c = c + sa * ((T)1 - sa * dtave) * W[p * M + k];
+                if constexpr (RP::FWAVE)  // sign(s) (1 - |s| dt/dx) Z
+                    c = c + sign_times((T)1 - sa * dtave, s[p]) * W[p * M + k];
+                else
+                    c = c + sa * ((T)1 - sa * dtave) * W[p * M + k];
             }
             cq[k] = c;
         }

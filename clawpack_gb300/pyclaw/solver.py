@@ -119,7 +119,7 @@ class ClawSolver2D:
             cc = float(pd["cc"]) if "cc" in pd else math.sqrt(bulk / rho)
             zz = float(pd["zz"]) if "zz" in pd else rho * cc
             return [rho, bulk, cc, zz]
-        if rp == _lib.RP_SHALLOW_ROE_WITH_EFIX_2D:
+        if rp in (_lib.RP_SHALLOW_ROE_WITH_EFIX_2D, _lib.RP_SHALLOW_BATHYMETRY_FWAVE_2D):
             return [float(pd["grav"])]
         if rp == _lib.RP_VC_ACOUSTICS_2D:
             return []  # the medium is in state.aux
@@ -132,8 +132,9 @@ class ClawSolver2D:
             raise NotImplementedError(
                 f"kernel_language={self.kernel_language!r}: this framework provides the 'CUDA' "
                 "backend only")
-        if self.fwave:
-            raise NotImplementedError("fwave is not supported")
+        rp_fwave = getattr(self.rp, "fwave", False)
+        if bool(self.fwave) != rp_fwave:
+            raise ValueError(f"{self.rp.name} needs solver.fwave = {rp_fwave}")
         if self.step_source is not None and self.source_split not in (1, 2):
             raise ValueError("solver.source_split must be 1 (Godunov) or 2 (Strang)")
         if self.num_ghost != 2:

@@ -15,12 +15,12 @@ from .. import _lib
 from . import static
 
 
-def _descriptor(name, rp_id):
+def _descriptor(name, rp_id, fwave=False):
     # cparam plays the role of the f2py module's Fortran common block, which
     # PyClaw fills from state.problem_data before stepping.
     return SimpleNamespace(__name__=f"clawpack_gb300.riemann.{name}", name=name, rp_id=rp_id,
                            num_eqn=static.num_eqn[name], num_waves=static.num_waves[name],
-                           num_aux=static.num_aux[name], cparam=SimpleNamespace())
+                           num_aux=static.num_aux[name], fwave=fwave, cparam=SimpleNamespace())
 
 
 acoustics_2D = _descriptor("acoustics_2D", _lib.RP_ACOUSTICS_2D)
@@ -29,6 +29,10 @@ shallow_roe_with_efix_2D = _descriptor("shallow_roe_with_efix_2D",
 euler_4wave_2D = _descriptor("euler_4wave_2D", _lib.RP_EULER_4WAVE_2D)
 # variable-coefficient acoustics: state.aux = (rho, c) per cell
 vc_acoustics_2D = _descriptor("vc_acoustics_2D", _lib.RP_VC_ACOUSTICS_2D)
+# shallow water over bathymetry, f-wave form (solver.fwave = True): state.aux =
+# (b,) per cell
+shallow_bathymetry_fwave_2D = _descriptor("shallow_bathymetry_fwave_2D",
+                                          _lib.RP_SHALLOW_BATHYMETRY_FWAVE_2D, fwave=True)
 
 __all__ = ["acoustics_2D", "shallow_roe_with_efix_2D", "euler_4wave_2D", "vc_acoustics_2D",
-           "static"]
+           "shallow_bathymetry_fwave_2D", "static"]

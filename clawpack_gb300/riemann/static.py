@@ -4,16 +4,19 @@ num_eqn = {
     "shallow_roe_with_efix_2D": 3,
     "euler_4wave_2D": 4,
     "vc_acoustics_2D": 3,
+    "shallow_bathymetry_fwave_2D": 3,
 }
 num_aux = {
     "acoustics_2D": 0,
     "shallow_roe_with_efix_2D": 0,
     "euler_4wave_2D": 0,
     "vc_acoustics_2D": 2,
+    "shallow_bathymetry_fwave_2D": 1,
 }
 num_waves = {
     "acoustics_2D": 2,
     "shallow_roe_with_efix_2D": 3,
     "euler_4wave_2D": 4,
     "vc_acoustics_2D": 2,
+    "shallow_bathymetry_fwave_2D": 3,
 }

@@ -35,6 +35,9 @@ extern "C" {
 #define GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D 2 /* m=3 (h,hu,hv), 3 waves; pd: grav */
 #define GCLAW_RP_EULER_4WAVE_2D 3           /* m=4 (rho,rhou,rhov,E), 4 waves; pd: gamma, efix */
 #define GCLAW_RP_VC_ACOUSTICS_2D 4          /* m=3 (p,u,v), 2 waves; aux (rho, c) per cell */
+/* shallow_bathymetry_fwave_2D: m=3 (h,hu,hv), 3 f-waves; aux (b) per cell, the
+ * bottom elevation; pd: grav.  Depths must stay positive (no dry cells). */
+#define GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D 5
 
 /* Boundary conditions: the values of pyclaw.BC. */
 #define GCLAW_BC_CUSTOM 0 /* not supported: rejected with GCLAW_ERR_UNSUPPORTED */
@@ -78,8 +81,9 @@ typedef struct gclaw_solver {
     int transverse_waves;         /* 0, 1 or 2 (solver.transverse_waves) */
     int precision;                /* GCLAW_PREC_* */
     double problem_data[8];       /* state.problem_data, layout per GCLAW_RP_* */
-    /* Solvers with an aux array (GCLAW_RP_VC_ACOUSTICS_2D): device pointer to
-     * aux, laid out like q with maux = 2 components -- (maux, mx, my), or
+    /* Solvers with an aux array (GCLAW_RP_VC_ACOUSTICS_2D, maux = 2;
+     * GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D, maux = 1): device pointer to
+     * aux, laid out like q with maux components -- (maux, mx, my), or
      * (maux, mx+4, my+4) with ghost cells filled for gclaw_step2 -- and its
      * boundary conditions (state.aux; solver.aux_bc_lower / aux_bc_upper;
      * walls mirror without negation).  Ignored by the other solvers; a

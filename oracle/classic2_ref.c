@@ -18,6 +18,7 @@
  *     riemann/src/rpn2_shallow_roe_with_efix.f90, rpt2_shallow_roe_with_efix.f90
  *     riemann/src/rpn2_euler_4wave.f90, rpt2_euler.f90
  *     riemann/src/rpn2_vc_acoustics.f90, rpt2_vc_acoustics.f90
+ *     riemann/src/rpn2_shallow_bathymetry_fwave.f90 (f-wave solver)
  * It is a restatement, in original code, of the published method that the
  * reference names as its algorithm source (CITATION.md:19-41):
  * R. J. LeVeque, J. Comput. Phys. 131 (1997) 327-353, and LeVeque, "Finite
@@ -48,6 +49,7 @@
 #define RP_SHALLOW_ROE_EFIX 2
 #define RP_EULER_4WAVE 3
 #define RP_VC_ACOUSTICS 4
+#define RP_SHALLOW_BATHY_FWAVE 5
 
 #define BC_CUSTOM 0
 #define BC_EXTRAP 1
@@ -73,6 +75,7 @@ static int rp_shape(int id, int *m, int *mw)
     case RP_SHALLOW_ROE_EFIX: *m = 3; *mw = 3; return 0;
     case RP_EULER_4WAVE: *m = 4; *mw = 4; return 0;
     case RP_VC_ACOUSTICS: *m = 3; *mw = 2; return 0;
+    case RP_SHALLOW_BATHY_FWAVE: *m = 3; *mw = 3; return 0;
     default: return ERR_ARG;
     }
 }
@@ -319,6 +322,63 @@ static int rpn2_vc_acoustics(int ixy, const double *ql, const double *qr, const 
     return 0;
 }
 
+/* Shallow water over bathymetry b = aux[0], f-wave form (Bale, LeVeque,
+ * Mitran and Rossmanith, SIAM J. Sci. Comput. 24 (2002) 955-978; FVMHP
+ * sec. 15.5; upstream rpn2_shallow_bathymetry_fwave.f90): the flux
+ * difference plus the bathymetry source, delta = f(qr) - f(ql) +
+ * (0, g hbar (br - bl), 0), is split into f-waves Z_p = beta_p r_p along the
+ * eigenvectors of the Roe matrix (the Roe averages of rpn2_shallow).
+ * amdq / apdq sum the f-waves of negative / positive speed (half each at
+ * speed zero).  A still lake (h + b constant, u = v = 0) has delta = 0, so
+ * it stays at rest.  Dry or negative depths are non-physical here. */
+static int rpn2_shallow_fwave(const rp_t *rp, int ixy, const double *ql, const double *qr,
+                              const double *al, const double *ar, double *wave, double *s,
+                              double *amdq, double *apdq)
+{
+    const double g = rp->pd[0];
+    const int mu = ixy, mv = 3 - ixy;
+    double hl = ql[0], hr = qr[0];
+    if (!(hl > 0.0) || !(hr > 0.0)) {
+        for (int k = 0; k < 9; k++) wave[k] = 0.0;
+        for (int k = 0; k < 3; k++) s[k] = amdq[k] = apdq[k] = 0.0;
+        return 1;
+    }
+    double hsqrtl = sqrt(hl), hsqrtr = sqrt(hr);
+    double hsq2 = hsqrtl + hsqrtr;
+    double ubar = (ql[mu] / hsqrtl + qr[mu] / hsqrtr) / hsq2;
+    double vbar = (ql[mv] / hsqrtl + qr[mv] / hsqrtr) / hsq2;
+    double hbar = (hl + hr) * 0.5;
+    double cbar = sqrt(g * hbar);
+    double ul = ql[mu] / hl, vl = ql[mv] / hl, ur = qr[mu] / hr, vr = qr[mv] / hr;
+    double d0 = qr[mu] - ql[mu];
+    double d1 = (qr[mu] * ur + 0.5 * g * hr * hr) - (ql[mu] * ul + 0.5 * g * hl * hl) +
+                g * hbar * (ar[0] - al[0]);
+    double d2 = qr[mu] * vr - ql[mu] * vl;
+    s[0] = ubar - cbar;
+    s[1] = ubar;
+    s[2] = ubar + cbar;
+    double b1 = (s[2] * d0 - d1) / (s[2] - s[0]);
+    double b3 = (d1 - s[0] * d0) / (s[2] - s[0]);
+    double b2 = d2 - vbar * d0;
+    double *z1 = wave, *z2 = wave + 3, *z3 = wave + 6;
+    z1[0] = b1; z1[mu] = b1 * s[0]; z1[mv] = b1 * vbar;
+    z2[0] = 0.0; z2[mu] = 0.0; z2[mv] = b2;
+    z3[0] = b3; z3[mu] = b3 * s[2]; z3[mv] = b3 * vbar;
+    for (int k = 0; k < 3; k++) amdq[k] = apdq[k] = 0.0;
+    for (int p = 0; p < 3; p++)
+        for (int k = 0; k < 3; k++) {
+            if (s[p] < 0.0) {
+                amdq[k] = amdq[k] + wave[3 * p + k];
+            } else if (s[p] > 0.0) {
+                apdq[k] = apdq[k] + wave[3 * p + k];
+            } else {
+                amdq[k] = amdq[k] + 0.5 * wave[3 * p + k];
+                apdq[k] = apdq[k] + 0.5 * wave[3 * p + k];
+            }
+        }
+    return 0;
+}
+
 /* al / ar: aux of the cells left / right of the edge (solvers with aux). */
 static int rpn2(const rp_t *rp, int ixy, const double *ql, const double *qr,
                 const double *al, const double *ar, double *wave, double *s, double *amdq,
@@ -328,6 +388,8 @@ static int rpn2(const rp_t *rp, int ixy, const double *ql, const double *qr,
     case RP_ACOUSTICS: return rpn2_acoustics(rp, ixy, ql, qr, wave, s, amdq, apdq);
     case RP_SHALLOW_ROE_EFIX: return rpn2_shallow(rp, ixy, ql, qr, wave, s, amdq, apdq);
     case RP_VC_ACOUSTICS: return rpn2_vc_acoustics(ixy, ql, qr, al, ar, wave, s, amdq, apdq);
+    case RP_SHALLOW_BATHY_FWAVE:
+        return rpn2_shallow_fwave(rp, ixy, ql, qr, al, ar, wave, s, amdq, apdq);
     default: return rpn2_euler(rp, ixy, ql, qr, wave, s, amdq, apdq);
     }
 }
@@ -448,7 +510,8 @@ static void rpt2(const rp_t *rp, int ixy, const double *ql, const double *qr,
 {
     switch (rp->id) {
     case RP_ACOUSTICS: rpt2_acoustics(rp, ixy, ql, qr, asdq, bm, bp); return;
-    case RP_SHALLOW_ROE_EFIX: rpt2_shallow(rp, ixy, ql, qr, asdq, bm, bp); return;
+    case RP_SHALLOW_ROE_EFIX:
+    case RP_SHALLOW_BATHY_FWAVE: rpt2_shallow(rp, ixy, ql, qr, asdq, bm, bp); return;
     case RP_VC_ACOUSTICS: rpt2_vc_acoustics(ixy, am, a0, ap, asdq, bm, bp); return;
     default: rpt2_euler(rp, ixy, ql, qr, asdq, bm, bp); return;
     }
@@ -554,13 +617,19 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
                 for (k = 0; k < m; k++) W(e)[p * m + k] = phi * W(e)[p * m + k];
             }
         }
+        /* correction flux: |s| (1 - |s| dt/dx) W for waves, sign(s) (1 - |s|
+         * dt/dx) Z for f-waves (the f-wave already carries the speed) */
+        const int fwave = rp->id == RP_SHALLOW_BATHY_FWAVE;
         double dtdxave = 0.5 * (dtdx + dtdx);
         for (e = 0; e <= n; e++)
             for (k = 0; k < m; k++) {
                 double c = 0.0;
                 for (p = 0; p < mw; p++) {
                     double sa = fabs(S(e)[p]);
-                    c = c + sa * (1.0 - sa * dtdxave) * W(e)[p * m + k];
+                    if (fwave)
+                        c = c + copysign(1.0, S(e)[p]) * (1.0 - sa * dtdxave) * W(e)[p * m + k];
+                    else
+                        c = c + sa * (1.0 - sa * dtdxave) * W(e)[p * m + k];
                 }
                 CQ(e)[k] = c;
                 A1(fadd, e)[k] = A1(fadd, e)[k] + 0.5 * c;
@@ -699,7 +768,8 @@ int gclaw_ref_rpn2(int rp_id, const double *pd, int ixy, const double *ql, const
     rp_t rp;
     rp.id = rp_id;
     if (rp_shape(rp_id, &rp.m, &rp.mw) || (ixy != 1 && ixy != 2)) return ERR_ARG;
-    if (rp_id == RP_VC_ACOUSTICS) return ERR_ARG; /* needs aux: gclaw_ref_rpn2_aux */
+    /* solvers with aux: gclaw_ref_rpn2_aux */
+    if (rp_id == RP_VC_ACOUSTICS || rp_id == RP_SHALLOW_BATHY_FWAVE) return ERR_ARG;
     memcpy(rp.pd, pd, sizeof rp.pd);
     return rpn2(&rp, ixy, ql, qr, NULL, NULL, wave, s, amdq, apdq) ? ERR_NONPHYSICAL : 0;
 }
@@ -758,7 +828,8 @@ int gclaw_ref_step2(int rp_id, const double *pd, int g, int mx, int my, const do
                     double *qnew, double dx, double dy, double dt, int order, int tw,
                     const int *mthlim, double *cfl_out, int nthreads)
 {
-    if (rp_id == RP_VC_ACOUSTICS) return ERR_ARG; /* needs aux: gclaw_ref_step2_aux */
+    /* solvers with aux: gclaw_ref_step2_aux */
+    if (rp_id == RP_VC_ACOUSTICS || rp_id == RP_SHALLOW_BATHY_FWAVE) return ERR_ARG;
     return step2_dirs(rp_id, pd, g, mx, my, qold, qnew, dx, dy, dt, order, tw, mthlim, cfl_out,
                       nthreads, 1, 2, 0, NULL);
 }
@@ -784,7 +855,7 @@ int gclaw_ref_step2ds(int rp_id, const double *pd, int g, int mx, int my, const 
                       const int *mthlim, int ixy, double *cfl_out, int nthreads)
 {
     if (ixy != 1 && ixy != 2) return ERR_ARG;
-    if (rp_id == RP_VC_ACOUSTICS) return ERR_ARG;
+    if (rp_id == RP_VC_ACOUSTICS || rp_id == RP_SHALLOW_BATHY_FWAVE) return ERR_ARG;
     return step2_dirs(rp_id, pd, g, mx, my, qold, qnew, dx, dy, dt, order, 0, mthlim, cfl_out,
                       nthreads, ixy, ixy, 0, NULL);
 }

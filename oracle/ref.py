@@ -20,8 +20,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libclassic2_ref.so")
 
-RP_ACOUSTICS, RP_SHALLOW, RP_EULER, RP_VC_ACOUSTICS = 1, 2, 3, 4
-SHAPES = {RP_ACOUSTICS: (3, 2), RP_SHALLOW: (3, 3), RP_EULER: (4, 4), RP_VC_ACOUSTICS: (3, 2)}
+RP_ACOUSTICS, RP_SHALLOW, RP_EULER, RP_VC_ACOUSTICS, RP_SHALLOW_FWAVE = 1, 2, 3, 4, 5
+SHAPES = {RP_ACOUSTICS: (3, 2), RP_SHALLOW: (3, 3), RP_EULER: (4, 4), RP_VC_ACOUSTICS: (3, 2),
+          RP_SHALLOW_FWAVE: (3, 3)}
 
 _lib = None
 

@@ -131,3 +131,17 @@ def test_aux_solver_needs_aux_pointer_and_aux_bcs():
     m, mw = ctypes.c_int(), ctypes.c_int()
     assert L.gclaw_rp_shape(_lib.RP_VC_ACOUSTICS_2D, ctypes.byref(m), ctypes.byref(mw)) == 0
     assert (m.value, mw.value) == (3, 2)
+
+
+def test_fwave_solver_shape_and_checks():
+    L = _lib.lib()
+    FW = _lib.RP_SHALLOW_BATHYMETRY_FWAVE_2D
+    m, mw = ctypes.c_int(), ctypes.c_int()
+    assert L.gclaw_rp_shape(FW, ctypes.byref(m), ctypes.byref(mw)) == 0
+    assert (m.value, mw.value) == (3, 3)
+    s = make_solver_struct(FW, 8, 8, 0.1, 0.1, [1, 1], [1, 1], [4] * 3, 2, 2, 0, [9.81])
+    assert L.gclaw_check(ctypes.byref(s)) == _lib.ERR_ARG  # no aux array
+    s.aux = 0x100000
+    assert L.gclaw_check(ctypes.byref(s)) == 0
+    s.problem_data[0] = 0.0  # gravity must be positive
+    assert L.gclaw_check(ctypes.byref(s)) == _lib.ERR_ARG

@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from clawpack_gb300 import pyclaw, riemann, workloads
+from clawpack_gb300 import _lib, pyclaw, riemann, workloads
 
 
 def test_solver_defaults_follow_pyclaw():
@@ -91,3 +91,28 @@ def test_batch_table_size():
     L = _lib.lib()
     assert L.gclaw_batch_table_bytes(10) == 10 * 48 + 2 * 11 * 4  # entries, tile and strip starts
     assert L.gclaw_batch_table_bytes(0) == 0
+
+
+def test_fwave_solver_front_end():
+    x = pyclaw.Dimension(0.0, 1.0, 8, name="x")
+    y = pyclaw.Dimension(0.0, 1.0, 6, name="y")
+    domain = pyclaw.Domain([x, y])
+    st = pyclaw.State(domain, 3, 1)
+    st.problem_data["grav"] = 9.81
+    st.aux[0] = -1.0
+    st.q[0] = 1.0
+    s = pyclaw.ClawSolver2D(riemann.shallow_bathymetry_fwave_2D)
+    s.dimensional_split = False
+    s.bc_lower = s.bc_upper = [pyclaw.BC.wall, pyclaw.BC.wall]
+    s.aux_bc_lower = s.aux_bc_upper = [pyclaw.BC.wall, pyclaw.BC.wall]
+    with pytest.raises(ValueError):  # f-wave solvers need solver.fwave = True
+        s.solver_struct(st)
+    s.fwave = True
+    ss = s.solver_struct(st)
+    assert ss.rp == _lib.RP_SHALLOW_BATHYMETRY_FWAVE_2D and ss.problem_data[0] == 9.81
+    assert s.num_waves == 3
+    s2 = pyclaw.ClawSolver2D(riemann.shallow_roe_with_efix_2D)
+    s2.fwave = True
+    claw = workloads.make_claw(workloads.shallow_dam_break(8, 8))
+    with pytest.raises(ValueError):  # and the other solvers fwave = False
+        s2.solver_struct(claw.solution.state)
