@@ -57,6 +57,7 @@ class GclawSolver(ctypes.Structure):
         ("aux", ctypes.c_void_p),
         ("aux_bc_lower", ctypes.c_int * 2),
         ("aux_bc_upper", ctypes.c_int * 2),
+        ("capa", ctypes.c_int),
     ]
 
 

@@ -449,7 +449,7 @@ extern "C" int gclaw_adjoint_step(const gclaw_solver *s, const double *q_dev,
     if (rc) return rc;
     if (!q_dev || !lam_new_dev || !lam_old_dev || lam_new_dev == lam_old_dev || !(dt > 0.0))
         return GCLAW_ERR_ARG;
-    if (s->rp != GCLAW_RP_ACOUSTICS_2D && s->rp != GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D)
+    if ((s->rp != GCLAW_RP_ACOUSTICS_2D && s->rp != GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D) || s->capa)
         return GCLAW_ERR_UNSUPPORTED;
     int m, mw;
     gclaw_rp_shape(s->rp, &m, &mw);

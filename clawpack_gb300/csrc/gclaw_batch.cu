@@ -388,7 +388,7 @@ int gclaw_batch_advance(const gclaw_solver *s, const void *table_dev, int nprob,
     // (the same choice as for single problems, so batched and single runs
     // of a problem agree bit for bit)
     const int fam = gclaw_fp32_kernel(-1);
-    if (rp_user_aux(s->rp)) return GCLAW_ERR_UNSUPPORTED;  // no per-problem aux
+    if (rp_user_aux(s->rp) || s->capa) return GCLAW_ERR_UNSUPPORTED;  // no per-problem aux
     if (!f64 && fam != 1) {
         switch (s->rp) {
         case GCLAW_RP_ACOUSTICS_2D:

@@ -164,7 +164,7 @@ template <typename T>
 struct RpAcoustics {
     static constexpr int M = 3, MW = 2, NR = 0, NA = 0, NUA = 0;
     static constexpr bool TNB = false;  // rpn2 does not read the transverse neighbours
-    static constexpr bool FWAVE = false;
+    static constexpr bool FWAVE = false, CAPA = false;
     struct Params {
         T cc, zz;
     };
@@ -223,7 +223,7 @@ struct RpAcoustics {
 template <typename T>
 struct RpVcAcoustics {
     static constexpr int M = 3, MW = 2, NR = 10, NA = 2, NUA = 2;
-    static constexpr bool TNB = true, FWAVE = false;
+    static constexpr bool TNB = true, FWAVE = false, CAPA = false;
     struct Params {
         int unused;
     };
@@ -301,7 +301,7 @@ __device__ __forceinline__ void split_sum(const T *sb, const T *wb, T *bm, T *bp
 template <typename T>
 struct RpShallow {
     static constexpr int M = 3, MW = 3, NR = 4, NA = 6, NUA = 0;
-    static constexpr bool TNB = false, FWAVE = false;
+    static constexpr bool TNB = false, FWAVE = false, CAPA = false;
     struct Params {
         T g;
         double gd;
@@ -497,7 +497,7 @@ struct RpShallow {
 template <typename T>
 struct RpShallowFwave {
     static constexpr int M = 3, MW = 3, NR = 4, NA = 6, NUA = 1;
-    static constexpr bool TNB = false, FWAVE = true;
+    static constexpr bool TNB = false, FWAVE = true, CAPA = false;
     using Params = typename RpShallow<T>::Params;
     static Params make(const double *pd) { return RpShallow<T>::make(pd); }
 
@@ -592,7 +592,7 @@ struct RpShallowFwave {
 template <typename T>
 struct RpEuler {
     static constexpr int M = 4, MW = 4, NR = 7, NA = 8, NUA = 0;
-    static constexpr bool TNB = false, FWAVE = false;
+    static constexpr bool TNB = false, FWAVE = false, CAPA = false;
     struct Params {
         T gamma, gamma1;
         int efix;

@@ -81,8 +81,10 @@ __global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1) step_kernel(const StepA
         const unsigned prev = atomicAdd(&c->blocks_done, 1u);
         if (prev == nblocks - 1) {
             __threadfence();
+            // with a capacity the tiles reduced Courant numbers, not speeds
+            constexpr bool CN = RPT<T>::CAPA;
             if (a.no_finish) c->blocks_done = 0u;
-            else finish_step(c, a.ctrl_mode, dt, dtdx, dtdy);
+            else finish_step(c, a.ctrl_mode, dt, CN ? 1.0 : dtdx, CN ? 1.0 : dtdy);
         }
     }
 }
@@ -279,8 +281,26 @@ static int launch_cfg(const gclaw_solver *s, const StepArgs &a, cudaStream_t st,
     return launch_tile<RPT, T, C::TX, C::TY, C::NT>(s, a, st, nlaunch);
 }
 
+// Capacity variants: FP64 tiles of the solver wrapped in Capa.
+template <template <typename> class RPT>
+static int launch_capa(const gclaw_solver *s, const StepArgs &a, cudaStream_t st, int nlaunch) {
+    using C = CapaTileCfg<RPT, double>;
+    return launch_tile<Capa<RPT>::template rp, double, C::TX, C::TY, C::NT>(s, a, st, nlaunch);
+}
+
 static int dispatch(const gclaw_solver *s, const StepArgs &a, cudaStream_t st, int nlaunch) {
     const bool f64 = s->precision == GCLAW_PREC_FP64;
+    if (s->capa) {
+        switch (s->rp) {
+        case GCLAW_RP_ACOUSTICS_2D: return launch_capa<RpAcoustics>(s, a, st, nlaunch);
+        case GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D: return launch_capa<RpShallow>(s, a, st, nlaunch);
+        case GCLAW_RP_EULER_4WAVE_2D: return launch_capa<RpEuler>(s, a, st, nlaunch);
+        case GCLAW_RP_VC_ACOUSTICS_2D: return launch_capa<RpVcAcoustics>(s, a, st, nlaunch);
+        case GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D:
+            return launch_capa<RpShallowFwave>(s, a, st, nlaunch);
+        default: return GCLAW_ERR_ARG;
+        }
+    }
     switch (s->rp) {
     case GCLAW_RP_ACOUSTICS_2D:
         return f64 ? launch_cfg<RpAcoustics, double>(s, a, st, nlaunch)
@@ -314,7 +334,8 @@ static void fill_args(const gclaw_solver *s, StepArgs &a) {
     for (int p = 0; p < 4; p++) a.mthlim |= (s->mthlim[p] & 0xff) << (8 * p);
     a.order = s->order;
     a.tw = s->transverse_waves;
-    a.aux = rp_user_aux(s->rp) ? s->aux : nullptr;
+    a.aux = (rp_user_aux(s->rp) || s->capa) ? s->aux : nullptr;
+    a.maux = rp_num_aux(s->rp) + (s->capa ? 1 : 0);
     for (int d = 0; d < 2; d++) {
         a.abc_lo[d] = s->aux_bc_lower[d];
         a.abc_hi[d] = s->aux_bc_upper[d];
@@ -377,6 +398,19 @@ int gclaw_check(const gclaw_solver *s) {
         return GCLAW_ERR_ARG;
     if (s->precision != GCLAW_PREC_FP64 && s->precision != GCLAW_PREC_FP32_BULK)
         return GCLAW_ERR_ARG;
+    if (s->capa) {
+        // kappa is the field after the solver's own; FP64 only
+        if (s->capa != rp_num_aux(s->rp) + 1 || !s->aux) return GCLAW_ERR_ARG;
+        if (s->precision != GCLAW_PREC_FP64) return GCLAW_ERR_UNSUPPORTED;
+        for (int d = 0; d < 2; d++) {
+            if (s->aux_bc_lower[d] < GCLAW_BC_EXTRAP || s->aux_bc_lower[d] > GCLAW_BC_WALL ||
+                s->aux_bc_upper[d] < GCLAW_BC_EXTRAP || s->aux_bc_upper[d] > GCLAW_BC_WALL)
+                return GCLAW_ERR_ARG;
+            if ((s->aux_bc_lower[d] == GCLAW_BC_PERIODIC) !=
+                (s->aux_bc_upper[d] == GCLAW_BC_PERIODIC))
+                return GCLAW_ERR_ARG;
+        }
+    }
     const double *pd = s->problem_data;
     switch (s->rp) {
     case GCLAW_RP_ACOUSTICS_2D:
@@ -516,7 +550,7 @@ int gclaw_step_split(const gclaw_solver *s, const double *q_dev, double *qnew_de
     int rc = gclaw_check(s);
     if (rc) return rc;
     if (!q_dev || !qnew_dev || !qtmp_dev || !ws_dev || !(dt > 0.0)) return GCLAW_ERR_ARG;
-    if (rp_user_aux(s->rp)) return GCLAW_ERR_UNSUPPORTED;
+    if (rp_user_aux(s->rp) || s->capa) return GCLAW_ERR_UNSUPPORTED;
     if (qtmp_dev == q_dev || qtmp_dev == qnew_dev || q_dev == qnew_dev) return GCLAW_ERR_ARG;
     StepArgs a{};
     fill_args(s, a);
@@ -534,7 +568,7 @@ int gclaw_advance_split(const gclaw_solver *s, double *q0_dev, double *q1_dev, d
     int rc = gclaw_check(s);
     if (rc) return rc;
     if (!q0_dev || !q1_dev || !qtmp_dev || !ctrl_dev || nsteps < 0) return GCLAW_ERR_ARG;
-    if (rp_user_aux(s->rp)) return GCLAW_ERR_UNSUPPORTED;
+    if (rp_user_aux(s->rp) || s->capa) return GCLAW_ERR_UNSUPPORTED;
     if (qtmp_dev == q0_dev || qtmp_dev == q1_dev || q0_dev == q1_dev) return GCLAW_ERR_ARG;
     StepArgs a{};
     fill_args(s, a);
@@ -773,6 +807,7 @@ extern "C" int gclaw_step2_noalloc(const gclaw_solver *s, const double *qold_dev
                                    double *qnew_dev, double dt, double *cfl_out, void *stream) {
     int rc = gclaw_check(s);
     if (rc) return rc;
+    if (s->capa) return GCLAW_ERR_UNSUPPORTED;
     // size first: a grid beyond the scratch is refused whatever the pointers
     const bool f64 = s->precision == GCLAW_PREC_FP64;
     int tx, ty;

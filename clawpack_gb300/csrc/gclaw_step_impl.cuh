@@ -24,7 +24,8 @@ struct StepArgs {
     int bc_lo[2], bc_hi[2];
     int mthlim;  // limiter id of wave p in bits 8p..8p+7
     int order, tw;
-    const double *aux;           // per-cell aux (solvers with NUA > 0), laid out like q
+    const double *aux;           // per-cell aux (user aux of the solver, then the capacity)
+    int maux;                    // fields per cell of aux, laid out like q
     int abc_lo[2], abc_hi[2];    // its boundary conditions (walls mirror, no negation)
     int sweeps;     // 1: x-sweep only, 2: y-sweep only (dimensional splitting); else both
     int no_finish;  // last block resets the block counter but leaves the CFL
@@ -74,13 +75,12 @@ __device__ __forceinline__ double load_q(const StepArgs &a, const double *__rest
 
 // Component k of the ghost-filled aux array at (gi, gj), as load_q maps q but
 // with the aux boundary conditions (a wall mirrors without negation).
-template <int NUA>
 __device__ __forceinline__ double load_a(const StepArgs &a, int k, int gi, int gj) {
     gi = min(max(gi, -2), a.mx + 1);
     gj = min(max(gj, -2), a.my + 1);
+    const size_t NUA = (size_t)a.maux;
     if (a.ghosted)
-        return __ldg(a.aux + k +
-                     (size_t)NUA * ((size_t)(gi + 2) + (size_t)(a.mx + 4) * (size_t)(gj + 2)));
+        return __ldg(a.aux + k + NUA * ((size_t)(gi + 2) + (size_t)(a.mx + 4) * (size_t)(gj + 2)));
     int sj = gj, si = gi;
     if (gj < 0) {
         const int b = a.abc_lo[1];
@@ -96,12 +96,43 @@ __device__ __forceinline__ double load_a(const StepArgs &a, int k, int gi, int g
         const int b = a.abc_hi[0];
         si = b == GCLAW_BC_EXTRAP ? a.mx - 1 : (b == GCLAW_BC_PERIODIC ? gi - a.mx : 2 * a.mx - 1 - gi);
     }
-    return __ldg(a.aux + k + (size_t)NUA * ((size_t)si + (size_t)a.mx * (size_t)sj));
+    return __ldg(a.aux + k + NUA * ((size_t)si + (size_t)a.mx * (size_t)sj));
 }
 
-// Solvers that read a user aux array (gclaw_solver.aux).
+// Solvers that read a user aux array (gclaw_solver.aux), and its fields.
 inline bool rp_user_aux(int rp) {
     return rp == GCLAW_RP_VC_ACOUSTICS_2D || rp == GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D;
+}
+inline int rp_num_aux(int rp) {
+    return rp == GCLAW_RP_VC_ACOUSTICS_2D ? 2 : (rp == GCLAW_RP_SHALLOW_BATHYMETRY_FWAVE_2D ? 1 : 0);
+}
+
+// Solver RPT with a capacity function kappa (classic2's mcapa): the user aux
+// array gains a last field, kappa, kept in aux-area plane KAP after the
+// solver's own planes.  The step then takes dt / (kappa dx) per cell for the
+// fluctuations, Courant numbers and transverse terms, the mean of an edge's
+// two cells in the correction flux, and divides the flux differences of a
+// cell by its kappa (capacity-form differencing, LeVeque 1997 sec. 5).
+template <template <typename> class RPT>
+struct Capa {
+    template <typename T>
+    struct rp : RPT<T> {
+        using B = RPT<T>;
+        static constexpr int NUA = B::NUA + 1, NA = B::NA + 1, KAP = B::NA;
+        static constexpr bool CAPA = true;
+        __device__ __forceinline__ static void cell_aux_user(const typename B::Params &P,
+                                                             const T *q, T *aux) {
+            if constexpr (B::NUA > 0) B::cell_aux_user(P, q, aux);
+            else if constexpr (B::NA > 0) B::cell_aux(P, q, aux);
+        }
+    };
+};
+
+// Aux-area plane of the capacity (solvers wrapped in Capa only).
+template <class RP>
+__host__ __device__ constexpr int capa_plane() {
+    if constexpr (RP::CAPA) return RP::KAP;
+    else return 0;
 }
 
 // Exact double <-> float conversions done with integer operations.  On
@@ -218,6 +249,17 @@ GCLAW_TILE_CFG(RpEuler, float, 24, 16, 384)
 #endif
 #undef GCLAW_TILE_CFG
 
+// Tile of the capacity variant: the solver's tile with TY lowered (by 2)
+// until the per-tile aux area, one plane larger, fits beside the rest.
+template <class RP, typename T, int TX, int TY>
+constexpr int capa_fit_ty();
+template <template <typename> class RPT, typename T>
+struct CapaTileCfg {
+    static constexpr int TX = TileCfg<RPT, T>::TX, NT = TileCfg<RPT, T>::NT;
+    static constexpr int TY =
+        capa_fit_ty<typename Capa<RPT>::template rp<T>, T, TX, TileCfg<RPT, T>::TY>();
+};
+
 // Cells per CTA of the kernel that runs solver rp at the given precision.
 static inline void tile_shape(int rp, int precision, int *tx, int *ty) {
     const bool f64 = precision == GCLAW_PREC_FP64;
@@ -304,6 +346,12 @@ struct Tile {
     }
 };
 
+template <class RP, typename T, int TX, int TY>
+constexpr int capa_fit_ty() {
+    if constexpr (TY <= 2 || Tile<RP, TX, TY>::template aux_own<T>()) return TY;
+    else return capa_fit_ty<RP, T, TX, TY - 2>();
+}
+
 // ---- phase 0: per-cell square roots and quotients for one sweep ---------
 template <class RP, typename T, int IXY, int TX, int TY, int NT>
 __device__ __forceinline__ void phase_aux(const typename RP::Params &P, const T *QS, T *CA) {
@@ -337,7 +385,7 @@ __device__ __forceinline__ void phase_aux(const typename RP::Params &P, const T 
 // ---- phase 1: normal Riemann problems on every edge of the sweep ---------
 template <class RP, typename T, int IXY, int TX, int TY, int NT>
 __device__ __forceinline__ void phase_rpn2(const typename RP::Params &P, const T *QS, const T *CA,
-                                           T *EA, int i0, int j0, int mx, int my, T &smax,
+                                           T *EA, int i0, int j0, int mx, int my, T dtdn, T &smax,
                                            bool &bad) {
     using TL = Tile<RP, TX, TY>;
     constexpr int M = RP::M, MW = RP::MW, NR = RP::NR, NA = RP::NA;
@@ -394,10 +442,21 @@ __device__ __forceinline__ void phase_rpn2(const typename RP::Params &P, const T
         for (int r = 0; r < NR; r++) EA[(TL::FR + r) * TL::NE1 + it] = R[r];
         const int ge = gbase_e + ea, gs = gbase_s + sl;
         if (ea >= 1 && ea <= NA1 - 2 && ge <= n && gs <= nt) {
+            if constexpr (RP::CAPA) {
+                // Courant numbers themselves: dt / (kappa dx) of the cell
+                // downwind of each wave, times |s|
+                const T dl = dtdn / CA[RP::KAP * TL::QN + cl], dr = dtdn / CA[RP::KAP * TL::QN + cr];
 #pragma unroll
-            for (int p = 0; p < MW; p++) {
-                bad |= isnan_v(s[p]);
-                smax = max_abs(smax, s[p]);
+                for (int p = 0; p < MW; p++) {
+                    bad |= isnan_v(s[p]);
+                    smax = max_abs(smax, gt0(s[p]) ? dr * s[p] : dl * s[p]);
+                }
+            } else {
+#pragma unroll
+                for (int p = 0; p < MW; p++) {
+                    bad |= isnan_v(s[p]);
+                    smax = max_abs(smax, s[p]);
+                }
             }
         }
     }
@@ -406,7 +465,7 @@ __device__ __forceinline__ void phase_rpn2(const typename RP::Params &P, const T
 // ---- phase 2: limiter, correction flux, transverse splitting -------------
 template <class RP, typename T, int IXY, int TX, int TY, int NT>
 __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const T *EA, T *EB,
-                                            int mthlim, int order, int tw, T dtdn) {
+                                            const T *CA, int mthlim, int order, int tw, T dtdn) {
     using TL = Tile<RP, TX, TY>;
     constexpr int M = RP::M, MW = RP::MW, NR = RP::NR;
     using SI = SweepIdx<IXY, TX, TY>;
@@ -465,7 +524,13 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
 #pragma unroll
                 for (int k = 0; k < M; k++) W[p * M + k] = phi * W[p * M + k];
             }
-            const T dtave = (T)0.5 * (dtdn + dtdn);
+            T dtave = (T)0.5 * (dtdn + dtdn);
+            if constexpr (RP::CAPA) {  // the mean dt / (kappa dx) of the edge's two cells
+                const int ea = e2 + 1;
+                const int cl = (IXY == 1) ? (sl + 1) * TL::QW + ea : ea * TL::QW + sl + 1;
+                const int cr = cl + ((IXY == 1) ? 1 : TL::QW);
+                dtave = (T)0.5 * (dtdn / CA[RP::KAP * TL::QN + cl] + dtdn / CA[RP::KAP * TL::QN + cr]);
+            }
 #pragma unroll
             for (int k = 0; k < M; k++) {
                 T c = (T)0;
@@ -520,8 +585,8 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
 // acc starts at q (FP64 mode) or 0 (FP32 mode) and receives, in order, the
 // slice-before term, the own-slice term and the slice-after term.
 template <class RP, typename T, typename A, int IXY, int TX, int TY, int NT, int NC>
-__device__ __forceinline__ void phase_accum(const T *EA, const T *EB, A (*acc)[RP::M], T dtdn,
-                                            T dtdt) {
+__device__ __forceinline__ void phase_accum(const T *EA, const T *EB, const T *CA,
+                                            A (*acc)[RP::M], T dtdn, T dtdt) {
     using TL = Tile<RP, TX, TY>;
     constexpr int M = RP::M;
     using SI = SweepIdx<IXY, TX, TY>;
@@ -538,6 +603,36 @@ __device__ __forceinline__ void phase_accum(const T *EA, const T *EB, A (*acc)[R
         // phase-2 area for the slice before, the own slice and the slice after
         const int el = SI::item1(al + 1, so), er = el + S1;
         const int b0 = SI::item2(al, so - 1), o0 = SI::item2(al, so), a0 = SI::item2(al, so + 1);
+        if constexpr (RP::CAPA) {
+            // capacity form: dt / (kappa dx) of the cell each term belongs
+            // to, and the flux differences over this cell's kappa
+            constexpr int TS = (IXY == 1) ? TL::QW : 1;
+            const int c0 = (cj + 2) * TL::QW + ci + 2;
+            const T *K = CA + RP::KAP * TL::QN;
+            const T ko = K[c0];
+            const T dto = dtdn / ko;
+            const T hb = (T)0.5 * (dtdn / K[c0 - TS]), ho = (T)0.5 * dto,
+                    ha = (T)0.5 * (dtdn / K[c0 + TS]);
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                const T *BMM = EB + (TL::GMM + k) * TL::NE2, *BPM = EB + (TL::GPM + k) * TL::NE2;
+                const T *BMP = EB + (TL::GMP + k) * TL::NE2, *BPP = EB + (TL::GPP + k) * TL::NE2;
+                const T *FA = EB + (TL::GFA + k) * TL::NE2;
+                const T g2b = ((T)0 - hb * BPM[b0 + S2]) - hb * BPP[b0];
+                const T qo = ((T)0 - dto * EA[(TL::FAP + k) * TL::NE1 + el]) -
+                             dto * EA[(TL::FAM + k) * TL::NE1 + er];
+                const T fo = FA[o0 + S2] - FA[o0];
+                const T g1o = ((T)0 - ho * BMM[o0 + S2]) - ho * BMP[o0];
+                const T g2o = ((T)0 - ho * BPM[o0 + S2]) - ho * BPP[o0];
+                const T g1a = ((T)0 - ha * BMM[a0 + S2]) - ha * BMP[a0];
+                A v = acc[t][k];
+                v = v + (A)dtdt * (A)g2b / (A)ko;
+                v = v + (A)qo - ((A)dtdn * (A)fo + (A)dtdt * ((A)g2o - (A)g1o)) / (A)ko;
+                v = v - (A)dtdt * (A)g1a / (A)ko;
+                acc[t][k] = v;
+            }
+            continue;
+        }
 #pragma unroll
         for (int k = 0; k < M; k++) {
             const T *BMM = EB + (TL::GMM + k) * TL::NE2, *BPM = EB + (TL::GPM + k) * TL::NE2;
@@ -670,8 +765,10 @@ __device__ __forceinline__ void load_tile(const StepArgs &a, const double *__res
         for (int idx = threadIdx.x; idx < (TX + 4) * TL::QH * RP::NUA; idx += NT) {
             const int k = idx % RP::NUA, cell = idx / RP::NUA;
             const int cx = cell % (TX + 4), cy = cell / (TX + 4);
-            CA[k * TL::QN + cy * TL::QW + cx] =
-                from_double<T>(load_a<RP::NUA>(a, k, i0 - 2 + cx, j0 - 2 + cy));
+            // the capacity (last user field) goes to its own plane
+            const int plane = (RP::CAPA && k == RP::NUA - 1) ? capa_plane<RP>() : k;
+            CA[plane * TL::QN + cy * TL::QW + cx] =
+                from_double<T>(load_a(a, k, i0 - 2 + cx, j0 - 2 + cy));
         }
     }
 }
@@ -728,11 +825,11 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, const typename RPT<
             phase_aux<RP, T, 1, TX, TY, NT>(P, QS, CA);
             __syncthreads();
         }
-        phase_rpn2<RP, T, 1, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, smax_x, bad);
+        phase_rpn2<RP, T, 1, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, tdtdx, smax_x, bad);
         __syncthreads();
-        phase_limit<RP, T, 1, TX, TY, NT>(P, EA, EB, a.mthlim, a.order, a.tw, tdtdx);
+        phase_limit<RP, T, 1, TX, TY, NT>(P, EA, EB, CA, a.mthlim, a.order, a.tw, tdtdx);
         __syncthreads();
-        phase_accum<RP, T, A, 1, TX, TY, NT, NC>(EA, EB, acc, tdtdx, tdtdy);
+        phase_accum<RP, T, A, 1, TX, TY, NT, NC>(EA, EB, CA, acc, tdtdx, tdtdy);
         if (do_y) __syncthreads();
     }
     if (do_y) {
@@ -740,11 +837,11 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, const typename RPT<
             phase_aux<RP, T, 2, TX, TY, NT>(P, QS, CA);
             __syncthreads();
         }
-        phase_rpn2<RP, T, 2, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, smax_y, bad);
+        phase_rpn2<RP, T, 2, TX, TY, NT>(P, QS, CA, EA, i0, j0, a.mx, a.my, tdtdy, smax_y, bad);
         __syncthreads();
-        phase_limit<RP, T, 2, TX, TY, NT>(P, EA, EB, a.mthlim, a.order, a.tw, tdtdy);
+        phase_limit<RP, T, 2, TX, TY, NT>(P, EA, EB, CA, a.mthlim, a.order, a.tw, tdtdy);
         __syncthreads();
-        phase_accum<RP, T, A, 2, TX, TY, NT, NC>(EA, EB, acc, tdtdy, tdtdx);
+        phase_accum<RP, T, A, 2, TX, TY, NT, NC>(EA, EB, CA, acc, tdtdy, tdtdx);
     }
 
     const int onx = a.ghosted ? a.mx + 4 : a.mx, ooff = a.ghosted ? 2 : 0;

@@ -21,7 +21,8 @@ def _stream_handle(stream=None):
 
 
 def make_solver_struct(rp_id, mx, my, dx, dy, bc_lower, bc_upper, mthlim, order, tw,
-                       precision, problem_data, aux_bc_lower=(1, 1), aux_bc_upper=(1, 1)):
+                       precision, problem_data, aux_bc_lower=(1, 1), aux_bc_upper=(1, 1),
+                       capa=0):
     s = _lib.GclawSolver()
     s.rp = int(rp_id)
     s.mx, s.my = int(mx), int(my)
@@ -41,6 +42,7 @@ def make_solver_struct(rp_id, mx, my, dx, dy, bc_lower, bc_upper, mthlim, order,
     for d in range(2):
         s.aux_bc_lower[d] = int(aux_bc_lower[d])
         s.aux_bc_upper[d] = int(aux_bc_upper[d])
+    s.capa = int(capa)
     return s
 
 

@@ -140,6 +140,15 @@ class ClawSolver2D:
         if self.num_ghost != 2:
             raise ValueError("num_ghost must be 2")
         need_aux = getattr(self.rp, "num_aux", 0)
+        capa = getattr(state, "index_capa", -1)
+        if capa >= 0:
+            if capa != need_aux:
+                raise NotImplementedError(
+                    f"the capacity must be the aux field after {self.rp.name}'s own "
+                    f"(state.index_capa = {need_aux})")
+            if self.precision != "fp64":
+                raise NotImplementedError("a capacity function needs solver.precision = 'fp64'")
+            need_aux += 1
         if state.num_aux != need_aux:
             raise ValueError(f"{self.rp.name} needs num_aux = {need_aux}, the state has "
                              f"{state.num_aux}")
@@ -172,9 +181,11 @@ class ClawSolver2D:
         prec = _lib.PREC_FP64 if self.precision == "fp64" else _lib.PREC_FP32_BULK
         abl = self.aux_bc_lower if state.num_aux else (1, 1)
         abu = self.aux_bc_upper if state.num_aux else (1, 1)
+        capa = getattr(state, "index_capa", -1)
         return make_solver_struct(self.rp.rp_id, mx, my, dx, dy, self.bc_lower, self.bc_upper,
                                   self._mthlim, self.order, self.transverse_waves, prec,
-                                  self._problem_data(state), abl, abu)
+                                  self._problem_data(state), abl, abu,
+                                  capa + 1 if capa >= 0 else 0)
 
     def setup(self, solution):
         self._check_options(solution.state)

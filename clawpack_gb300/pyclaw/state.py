@@ -20,6 +20,8 @@ class State:
             raise TypeError("State(domain_or_patch, num_eqn)")
         self.num_eqn = int(num_eqn)
         self.num_aux = int(num_aux)
+        # aux field holding the capacity function (-1: none), as in PyClaw
+        self.index_capa = -1
         self.problem_data = {}
         self.t = 0.0
         self.q = np.zeros([self.num_eqn] + self.patch.grid.num_cells, order="F")

@@ -90,6 +90,15 @@ typedef struct gclaw_solver {
      * zero-initialised tail means "no aux". */
     const double *aux;
     int aux_bc_lower[2], aux_bc_upper[2];
+    /* Capacity function (classic2's mcapa = state.index_capa + 1): 0 for
+     * none, else the 1-based index of the capacity field kappa in aux, which
+     * must be the field after the solver's own (maux = solver's + 1; for
+     * the solvers without aux, aux holds kappa alone).  The step then takes
+     * dt / (kappa dx) per cell and divides each cell's flux differences by
+     * its kappa.  FP64, unsplit steps with a workspace (gclaw_step,
+     * gclaw_step2, gclaw_advance and their host forms); refused with
+     * GCLAW_ERR_UNSUPPORTED elsewhere. */
+    int capa;
 } gclaw_solver;
 
 /* Time-step control block, resident in device memory.  The step kernel's

@@ -552,7 +552,7 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
                        int order, int tw, const int *mthlim,
                        double *qadd, double *fadd, double *g1, double *g2, double *cfl1d,
                        const work_t *wk, int maux, const double *auxm, const double *aux0,
-                       const double *auxp)
+                       const double *auxp, const double *kap)
 {
     const int m = rp->m, mw = rp->mw;
     const int off = 2;
@@ -567,6 +567,8 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
 #define BP(e) (wk->bp + (size_t)((e) + off) * m)
 #define A1(arr, c) ((arr) + (size_t)((c) + off) * m)
 #define AX(arr, c) ((arr) ? (arr) + (size_t)((c) + off) * maux : NULL)
+/* dtdx1d of flux2: dt/dx over the capacity of cell c (kap[c + off]) */
+#define DTDX(c) (kap ? dtdx / kap[(c) + off] : dtdx)
 
     for (e = -1; e <= n + 1; e++)
         bad |= rpn2(rp, ixy, Q(e - 1), Q(e), AX(aux0, e - 1), AX(aux0, e), W(e), S(e), AM(e),
@@ -583,8 +585,8 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
     /* first-order (Godunov) updates */
     for (e = 0; e <= n; e++)
         for (k = 0; k < m; k++) {
-            A1(qadd, e)[k] = A1(qadd, e)[k] - dtdx * AP(e)[k];
-            A1(qadd, e - 1)[k] = A1(qadd, e - 1)[k] - dtdx * AM(e)[k];
+            A1(qadd, e)[k] = A1(qadd, e)[k] - DTDX(e) * AP(e)[k];
+            A1(qadd, e - 1)[k] = A1(qadd, e - 1)[k] - DTDX(e - 1) * AM(e)[k];
         }
 
     /* Courant number over the edges of this slice */
@@ -592,7 +594,7 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
     for (e = 0; e <= n; e++)
         for (p = 0; p < mw; p++) {
             double sp = S(e)[p];
-            cfl = fmax(cfl, fmax(dtdx * sp, -dtdx * sp));
+            cfl = fmax(cfl, fmax(DTDX(e) * sp, -DTDX(e - 1) * sp));
         }
     *cfl1d = cfl;
 
@@ -620,9 +622,10 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
         /* correction flux: |s| (1 - |s| dt/dx) W for waves, sign(s) (1 - |s|
          * dt/dx) Z for f-waves (the f-wave already carries the speed) */
         const int fwave = rp->id == RP_SHALLOW_BATHY_FWAVE;
-        double dtdxave = 0.5 * (dtdx + dtdx);
         for (e = 0; e <= n; e++)
             for (k = 0; k < m; k++) {
+                /* dt/dx averaged over the edge's two cells */
+                double dtdxave = 0.5 * (DTDX(e - 1) + DTDX(e));
                 double c = 0.0;
                 for (p = 0; p < mw; p++) {
                     double sa = fabs(S(e)[p]);
@@ -643,12 +646,13 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
                     AM(e)[k] = AM(e)[k] + CQ(e)[k];
                     AP(e)[k] = AP(e)[k] - CQ(e)[k];
                 }
-        const double h = 0.5 * dtdx;
+        /* the half dt/dx of the cell the fluctuation goes into */
         for (e = 0; e <= n; e++)
             rpt2(rp, ixy, Q(e - 1), Q(e), AX(auxm, e - 1), AX(aux0, e - 1), AX(auxp, e - 1),
                  AM(e), BM(e), BP(e));
         for (e = 0; e <= n; e++)
             for (k = 0; k < m; k++) {
+                const double h = 0.5 * DTDX(e - 1);
                 A1(g1, e - 1)[k] = A1(g1, e - 1)[k] - h * BM(e)[k];
                 A1(g2, e - 1)[k] = A1(g2, e - 1)[k] - h * BP(e)[k];
             }
@@ -657,6 +661,7 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
                  BP(e));
         for (e = 0; e <= n; e++)
             for (k = 0; k < m; k++) {
+                const double h = 0.5 * DTDX(e);
                 A1(g1, e)[k] = A1(g1, e)[k] - h * BM(e)[k];
                 A1(g2, e)[k] = A1(g2, e)[k] - h * BP(e)[k];
             }
@@ -671,6 +676,7 @@ static int flux2_slice(const rp_t *rp, int ixy, int n, const double *q1d, double
 #undef BP
 #undef A1
 #undef AX
+#undef DTDX
     return bad;
 }
 
@@ -822,7 +828,7 @@ double gclaw_ref_philim(int id, double r) { return philim(id, r); }
 static int step2_dirs(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
                       double *qnew, double dx, double dy, double dt, int order, int tw,
                       const int *mthlim, double *cfl_out, int nthreads, int ixy_lo,
-                      int ixy_hi, int maux, const double *auxbc);
+                      int ixy_hi, int maux, const double *auxbc, int mcapa);
 
 int gclaw_ref_step2(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
                     double *qnew, double dx, double dy, double dt, int order, int tw,
@@ -831,19 +837,25 @@ int gclaw_ref_step2(int rp_id, const double *pd, int g, int mx, int my, const do
     /* solvers with aux: gclaw_ref_step2_aux */
     if (rp_id == RP_VC_ACOUSTICS || rp_id == RP_SHALLOW_BATHY_FWAVE) return ERR_ARG;
     return step2_dirs(rp_id, pd, g, mx, my, qold, qnew, dx, dy, dt, order, tw, mthlim, cfl_out,
-                      nthreads, 1, 2, 0, NULL);
+                      nthreads, 1, 2, 0, NULL, 0);
 }
 
-/* step2 for solvers with an aux array: auxbc is (maux, mx+2g, my+2g),
- * Fortran order, ghosts filled (gclaw_ref_fill_aux_ghosts). */
+/* step2 with an aux array: auxbc is (maux, mx+2g, my+2g), Fortran order,
+ * ghosts filled (gclaw_ref_fill_aux_ghosts).  mcapa: 1-based index of the
+ * capacity field in aux (classic2's mcapa, PyClaw state.index_capa + 1), 0
+ * for none; with a capacity kappa the step is the capacity-form update of
+ * LeVeque 1997 sec. 5 / FVMHP sec. 6.16: dt/dx becomes dt/(kappa dx) per
+ * cell (fluctuations, Courant numbers, transverse terms, and the average of
+ * the edge's two cells in the correction flux), and the flux differences of
+ * cell (i,j) are divided by its kappa. */
 int gclaw_ref_step2_aux(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
                         double *qnew, int maux, const double *auxbc, double dx, double dy,
                         double dt, int order, int tw, const int *mthlim, double *cfl_out,
-                        int nthreads)
+                        int nthreads, int mcapa)
 {
-    if (maux < 1 || maux > MAXM || !auxbc) return ERR_ARG;
+    if (maux < 1 || maux > MAXM || !auxbc || mcapa < 0 || mcapa > maux) return ERR_ARG;
     return step2_dirs(rp_id, pd, g, mx, my, qold, qnew, dx, dy, dt, order, tw, mthlim, cfl_out,
-                      nthreads, 1, 2, maux, auxbc);
+                      nthreads, 1, 2, maux, auxbc, mcapa);
 }
 
 /* One sweep of PyClaw's dimensionally split step (classic2 step2ds,
@@ -857,13 +869,13 @@ int gclaw_ref_step2ds(int rp_id, const double *pd, int g, int mx, int my, const 
     if (ixy != 1 && ixy != 2) return ERR_ARG;
     if (rp_id == RP_VC_ACOUSTICS || rp_id == RP_SHALLOW_BATHY_FWAVE) return ERR_ARG;
     return step2_dirs(rp_id, pd, g, mx, my, qold, qnew, dx, dy, dt, order, 0, mthlim, cfl_out,
-                      nthreads, ixy, ixy, 0, NULL);
+                      nthreads, ixy, ixy, 0, NULL, 0);
 }
 
 static int step2_dirs(int rp_id, const double *pd, int g, int mx, int my, const double *qold,
                       double *qnew, double dx, double dy, double dt, int order, int tw,
                       const int *mthlim, double *cfl_out, int nthreads, int ixy_lo, int ixy_hi,
-                      int maux, const double *auxbc)
+                      int maux, const double *auxbc, int mcapa)
 {
     rp_t rp;
     rp.id = rp_id;
@@ -909,10 +921,12 @@ static int step2_dirs(int rp_id, const double *pd, int g, int mx, int my, const 
             wk.cqxx = malloc(sizeof(double) * per);
             wk.bm = malloc(sizeof(double) * per);
             wk.bp = malloc(sizeof(double) * per);
-            /* aux of the slice and of the slices below and above it */
+            /* aux of the slice and of the slices below and above it, and the
+             * slice's capacities */
             double *a1d[3] = {NULL, NULL, NULL};
             if (maux)
                 for (int d = 0; d < 3; d++) a1d[d] = malloc(sizeof(double) * (size_t)nmax * maux);
+            double *k1d = mcapa ? malloc(sizeof(double) * (size_t)nmax) : NULL;
 #pragma omp for schedule(static)
             for (int sl = 0; sl < ns; sl++) {
                 /* slice index sl -> row j = sl-1 (x-sweep) or column i = sl-1 */
@@ -933,11 +947,14 @@ static int step2_dirs(int rp_id, const double *pd, int g, int mx, int my, const 
                             a1d[d][(size_t)(c + 2) * maux + k] = auxbc[src];
                         }
                 }
+                if (mcapa)
+                    for (int c = -2; c < n + 2; c++) k1d[c + 2] = a1d[1][(size_t)(c + 2) * maux + mcapa - 1];
                 bad |= flux2_slice(&rp, ixy, n, q1d, dtdn, order, tw, mthlim, QA + per * sl,
                                    FA + per * sl, G1 + per * sl, G2 + per * sl, &cfls[sl], &wk,
-                                   maux, a1d[0], a1d[1], a1d[2]);
+                                   maux, a1d[0], a1d[1], a1d[2], k1d);
             }
             for (int d = 0; d < 3; d++) free(a1d[d]);
+            free(k1d);
             free(q1d); free(wk.wave); free(wk.s); free(wk.amdq); free(wk.apdq);
             free(wk.cqxx); free(wk.bm); free(wk.bp);
         }
@@ -960,6 +977,19 @@ static int step2_dirs(int rp_id, const double *pd, int g, int mx, int my, const 
                 const double *fa1 = fa0 + m;
                 const double *g1o = G1 + per * sl + (size_t)(c + 2) * m;
                 const double *g2o = G2 + per * sl + (size_t)(c + 2) * m;
+                if (mcapa) {
+                    /* the flux differences and transverse terms over the
+                     * capacity of this cell */
+                    const double kc = auxbc[(size_t)(mcapa - 1) + (size_t)maux * (dst / m)];
+                    for (int k = 0; k < m; k++) {
+                        double v = qnew[dst + k];
+                        v = v + dtdt * g2prev[k] / kc;
+                        v = v + qa[k] - (dtdn * (fa1[k] - fa0[k]) + dtdt * (g2o[k] - g1o[k])) / kc;
+                        v = v - dtdt * g1next[k] / kc;
+                        qnew[dst + k] = v;
+                    }
+                    continue;
+                }
                 for (int k = 0; k < m; k++) {
                     double v = qnew[dst + k];
                     v = v + dtdt * g2prev[k];
@@ -1053,7 +1083,7 @@ int gclaw_ref_step_aux(int rp_id, const double *pd, int mx, int my, const double
                        double *qout, int maux, const double *aux, double dx, double dy,
                        double dt, int order, int tw, const int *mthlim, const int *bc_lower,
                        const int *bc_upper, const int *aux_bc_lower, const int *aux_bc_upper,
-                       double *cfl_out, int nthreads)
+                       double *cfl_out, int nthreads, int mcapa)
 {
     int m, mw;
     if (rp_shape(rp_id, &m, &mw) || maux < 1 || maux > MAXM) return ERR_ARG;
@@ -1069,7 +1099,7 @@ int gclaw_ref_step_aux(int rp_id, const double *pd, int mx, int my, const double
     if (rc == 0) rc = gclaw_ref_fill_aux_ghosts(maux, mx, my, g, aux_bc_lower, aux_bc_upper, aux, ab);
     if (rc == 0)
         rc = gclaw_ref_step2_aux(rp_id, pd, g, mx, my, qa, qb, maux, ab, dx, dy, dt, order, tw,
-                                 mthlim, cfl_out, nthreads);
+                                 mthlim, cfl_out, nthreads, mcapa);
     if (rc == 0 || rc == ERR_NONPHYSICAL)
         for (int j = 0; j < my; j++)
             for (int i = 0; i < mx; i++)

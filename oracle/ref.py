@@ -57,11 +57,11 @@ def lib():
         L.gclaw_ref_step_aux.argtypes = [ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, dp, dp,
                                          ctypes.c_int, dp, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double, ctypes.c_int, ctypes.c_int, ip, ip, ip,
-                                         ip, ip, dp, ctypes.c_int]
+                                         ip, ip, dp, ctypes.c_int, ctypes.c_int]
         L.gclaw_ref_step2_aux.argtypes = [ctypes.c_int, dp, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_int, dp, dp, ctypes.c_int, dp, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_int,
-                                          ctypes.c_int, ip, dp, ctypes.c_int]
+                                          ctypes.c_int, ip, dp, ctypes.c_int, ctypes.c_int]
         L.gclaw_ref_rpn2_aux.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp,
                                          dp, dp]
         L.gclaw_ref_rpt2_aux.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp]
@@ -136,9 +136,10 @@ def step(rp, pd, q, dx, dy, dt, bc_lower, bc_upper, order=2, tw=2, mthlim=(4, 4,
 
 
 def step_aux(rp, pd, q, aux, dx, dy, dt, bc_lower, bc_upper, aux_bc_lower, aux_bc_upper,
-             order=2, tw=2, mthlim=(4, 4, 4, 4), nthreads=1):
-    """Ghost fill of q and aux + step for solvers with an aux array (maux, mx,
-    my); returns (qnew, cfl, rc)."""
+             order=2, tw=2, mthlim=(4, 4, 4, 4), nthreads=1, mcapa=0):
+    """Ghost fill of q and aux + step with an aux array (maux, mx, my); mcapa
+    is the 1-based capacity field of aux (0: none).  Returns (qnew, cfl,
+    rc)."""
     m, mx, my = q.shape
     qf = np.asfortranarray(q, dtype=np.float64)
     af = np.asfortranarray(aux, dtype=np.float64)
@@ -150,7 +151,7 @@ def step_aux(rp, pd, q, aux, dx, dy, dt, bc_lower, bc_upper, aux_bc_lower, aux_b
     rc = lib().gclaw_ref_step_aux(rp, _dp(_pd(pd)), mx, my, _dp(qf), _dp(qout), af.shape[0],
                                   _dp(af), dx, dy, dt, order, tw, _ip(lim), i32(bc_lower),
                                   i32(bc_upper), i32(aux_bc_lower), i32(aux_bc_upper), _dp(cfl),
-                                  nthreads)
+                                  nthreads, mcapa)
     if rc < 0:
         raise ValueError(f"gclaw_ref_step_aux failed: {rc}")
     return qout, float(cfl[0]), rc
