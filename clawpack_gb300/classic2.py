@@ -7,9 +7,12 @@ pyclaw/src/pyclaw/classic/solver.py) calls
                              dx, dy, dt, method, mthlim, fwave, rpn2, rpt2)
 
 with ``qold``/``qbc`` of shape (num_eqn, mx+2*num_ghost, my+2*num_ghost) in
-Fortran order, ``method`` the 7-entry integer array (method[1] = order,
-method[2] = transverse_waves), ``mthlim`` the limiter id per wave and
-``rpn2``/``rpt2`` the Riemann solver module.  Pointing ``self.fmod`` at this
+Fortran order, ``auxbc`` the ghost-filled aux array (num_aux, mx+4, my+4)
+(or empty), ``method`` the 7-entry integer array (method[1] = order,
+method[2] = transverse_waves, method[5] = mcapa = state.index_capa + 1,
+method[6] = num_aux), ``mthlim`` the limiter id per wave, ``fwave`` whether
+the solver returns f-waves, and ``rpn2``/``rpt2`` the Riemann solver
+module.  Pointing ``self.fmod`` at this
 module runs the step on the GPU through ``gclaw_step2``: the arrays may be
 numpy (copied to and from the device each call, as the reference passes
 them) or CUDA torch tensors of shape (my+4, mx+4, num_eqn) that stay on the
@@ -44,9 +47,19 @@ def _problem_data(rp):
         cc = float(getattr(c, "cc", math.sqrt(bulk / rho)))
         zz = float(getattr(c, "zz", rho * cc))
         return [rho, bulk, cc, zz]
-    if rp.rp_id == _lib.RP_SHALLOW_ROE_WITH_EFIX_2D:
+    if rp.rp_id in (_lib.RP_SHALLOW_ROE_WITH_EFIX_2D, _lib.RP_SHALLOW_BATHYMETRY_FWAVE_2D):
         return [float(c.grav)]
+    if rp.rp_id == _lib.RP_VC_ACOUSTICS_2D:
+        return []
     return [float(c.gamma), 1.0 if getattr(c, "efix", True) else 0.0]
+
+
+def _device_array(a):
+    """A ghost-filled (n, mx+4, my+4) host array as the device layout
+    (my+4, mx+4, n), or a CUDA tensor already in that layout."""
+    if isinstance(a, torch.Tensor):
+        return a
+    return torch.from_numpy(np.ascontiguousarray(np.asfortranarray(a, dtype=np.float64).T)).cuda()
 
 
 def step2(maxm, num_ghost, mx, my, qold, qnew, aux, dx, dy, dt, method, mthlim, fwave, rpn2,
@@ -54,16 +67,20 @@ def step2(maxm, num_ghost, mx, my, qold, qnew, aux, dx, dy, dt, method, mthlim, 
     """One unsplit step; returns (qnew, cfl) like the f2py routine."""
     if num_ghost != 2:
         raise ValueError("num_ghost must be 2")
-    if fwave:
-        raise NotImplementedError("f-wave solvers are not supported")
-    if aux is not None and np.size(aux) > 0:
-        raise NotImplementedError("aux arrays are not supported")
+    if bool(fwave) != bool(getattr(rpn2, "fwave", False)):
+        raise ValueError(f"{rpn2.name} needs fwave = {bool(getattr(rpn2, 'fwave', False))}")
     order, tw = int(method[1]), int(method[2])
+    mcapa = int(method[5]) if len(method) > 5 else 0
     if tw < 0:
         raise NotImplementedError("dimensional splitting is not supported")
+    has_aux = aux is not None and (aux.numel() if isinstance(aux, torch.Tensor) else np.size(aux))
     # The ghost cells are already filled; bc ids only have to pass validation.
     s = make_solver_struct(rpn2.rp_id, mx, my, dx, dy, bc_lower, bc_upper, list(mthlim), order,
-                           tw, precision, _problem_data(rpn2))
+                           tw, precision, _problem_data(rpn2), capa=mcapa)
+    d_aux = None
+    if has_aux:
+        d_aux = _device_array(aux)  # stream-ordered: safe to drop after the launch
+        s.aux = d_aux.data_ptr()
     L = _lib.lib()
     cfl = ctypes.c_double()
     if isinstance(qold, torch.Tensor):

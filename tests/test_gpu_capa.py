@@ -201,3 +201,32 @@ def test_stretched_grid_through_pyclaw_front_end(cuda, oracle):
     # the physical mass, sum(kappa h), is conserved between walls
     m0 = (aux[0] * q0[0]).sum()
     assert abs((aux[0] * claw.frames[-1].q[0]).sum() - m0) <= 1e-12 * m0
+
+
+@pytest.mark.parametrize("rp,capa", [(VC, False), (FW, False), (FW, True), (2, True)])
+def test_f2py_shaped_step2_dropin_with_aux(cuda, oracle, rp, capa):
+    """clawpack_gb300.classic2.step2 called as PyClaw calls the f2py module
+    for solvers with aux, f-waves and a capacity (method[5] = mcapa)."""
+    from clawpack_gb300 import classic2
+
+    mod = {VC: riemann.vc_acoustics_2D, FW: riemann.shallow_bathymetry_fwave_2D,
+           2: riemann.shallow_roe_with_efix_2D}[rp]
+    if rp != VC:
+        mod.cparam.grav = PD[rp][0]
+    rng = np.random.default_rng(40 + rp + capa)
+    mx, my = 33, 21
+    q, aux = problem(rp, mx, my, rng)
+    if not capa:
+        aux = np.asfortranarray(aux[:-1])
+    bcl, bcu = [1, 3], [1, 3]
+    qbc = oracle.fill_ghosts(q, bcl, bcu)
+    auxbc = oracle.fill_aux_ghosts(aux, bcl, bcu)
+    mcapa = aux.shape[0] if capa else 0
+    method = np.array([1, 2, 2, 0, 1, mcapa, aux.shape[0]])
+    mw = SHAPES[rp][1]
+    out, cfl = classic2.step2(max(mx, my), 2, mx, my, qbc, qbc.copy(order="F"), auxbc, 0.05, 0.04,
+                              0.001, method, [4] * mw, rp == FW, mod, mod)
+    ref_q, ref_cfl, rc = oracle.step_aux(rp, PD[rp], q, aux, 0.05, 0.04, 0.001, bcl, bcu, bcl,
+                                         bcu, 2, 2, [4] * 4, mcapa=mcapa)
+    assert rel_l1(out[:, 2:-2, 2:-2], ref_q) <= 1e-13
+    assert abs(cfl - ref_cfl) <= 1e-14 * ref_cfl
