@@ -100,12 +100,36 @@ class GclawCtrl(ctypes.Structure):
 
 CTRL_BYTES = ctypes.sizeof(GclawCtrl)
 
-# Every symbol include/gclaw.h declares, with (restype, argtypes).
+# include/gclaw3.h: the unsplit 3D step
+RP3_ACOUSTICS_3D = 1
+
+
+class GclawSolver3(ctypes.Structure):
+    _fields_ = [
+        ("rp", ctypes.c_int),
+        ("mx", ctypes.c_int),
+        ("my", ctypes.c_int),
+        ("mz", ctypes.c_int),
+        ("dx", ctypes.c_double),
+        ("dy", ctypes.c_double),
+        ("dz", ctypes.c_double),
+        ("bc_lower", ctypes.c_int * 3),
+        ("bc_upper", ctypes.c_int * 3),
+        ("mthlim", ctypes.c_int * MAX_WAVES),
+        ("order", ctypes.c_int),
+        ("transverse_waves", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("problem_data", ctypes.c_double * 8),
+    ]
+
+# (restype, argtypes) of the C entry points.
 _P = ctypes.c_void_p
 _D = ctypes.c_double
 _I = ctypes.c_int
 _SZ = ctypes.c_size_t
 _SP = ctypes.POINTER(GclawSolver)
+_SP3 = ctypes.POINTER(GclawSolver3)
+# Every symbol include/gclaw.h and include/gclaw3.h declare.
 SIGNATURES = {
     "gclaw_version": (ctypes.c_char_p, []),
     "gclaw_strerror": (ctypes.c_char_p, [_I]),
@@ -130,6 +154,11 @@ SIGNATURES = {
     "gclaw_batch_advance": (_I, [_SP, _P, _I, _I, _P, _P, _P, _I, _P]),
     "gclaw_evolve_host": (_I, [_SP, _P, _P, _D, _D, _D, _I, _D, _D, _D, _I, _P, _SZ, _I,
                                ctypes.POINTER(GclawCtrl), _P]),
+    "gclaw3_rp_shape": (_I, [_I, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "gclaw3_check": (_I, [_SP3]),
+    "gclaw3_workspace_bytes": (_SZ, [_SP3]),
+    "gclaw3_step": (_I, [_SP3, _P, _P, _D, _P, _P, _P]),
+    "gclaw3_advance": (_I, [_SP3, _P, _P, _P, _P, _I, _P]),
 }
 
 _libs = {}

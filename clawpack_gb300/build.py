@@ -24,7 +24,7 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 SRC = [os.path.join(HERE, "csrc", n) for n in ("gclaw_step.cu", "gclaw_batch.cu",
-                                                 "gclaw_adjoint.cu")]
+                                                 "gclaw_adjoint.cu", "gclaw3.cu")]
 BUILD_DIR = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,0 +1,610 @@
+// gclaw3.cu -- the classic unsplit 3D wave-propagation step (PyClaw
+// ClawSolver3D / classic3 step3 + flux3; Langseth and LeVeque, J. Comput.
+// Phys. 165 (2000)) on GB300, FP64.
+//
+// One step is three sweeps (x, y, z); each sweep is three kernels over the
+// whole grid, staged through a caller-provided workspace in HBM:
+//   k_edges   one thread per edge: rpn3 of the two cells, storing the waves,
+//             speeds and fluctuations, and the sweep's Courant numbers;
+//   k_chains  one thread per edge: the limiter (against the neighbouring
+//             edges' unlimited waves along the sweep), the correction flux,
+//             and the transverse chains of A-dQ and A+dQ: rpt3 splits in
+//             both transverse directions and, with transverse_waves 11 or
+//             22, the rptt3 corner terms, stored as the values each chain
+//             adds to the transverse flux entries of its cell;
+//   k_update  one thread per cell: adds, in a fixed order, the first-order
+//             term, the correction-flux difference and the transverse-flux
+//             terms of the 3x3 slices around the cell.
+// Edge records live on the box of positions [-1, n+1]^3 (x fastest, one
+// field per plane), so consecutive threads touch consecutive x positions in
+// every sweep.  The operations and their order are those of the CPU oracle,
+// so the -fmad=false build reproduces it bit for bit.  The last block of the
+// z-sweep's update applies PyClaw's evolve_to_time rules to the gclaw_ctrl
+// block (finish_step), as the 2D step does.
+#include <cuda_runtime.h>
+
+#include "gclaw.h"
+#include "gclaw3.h"
+#include "gclaw_step_impl.cuh"
+
+namespace gclaw {
+namespace g3 {
+
+constexpr int NT3 = 256;
+
+struct Args3 {
+    const double *qin[2];
+    double *qout[2];
+    gclaw_ctrl *ctrl;
+    double *ws;
+    double dt, d[3];
+    int n[3];
+    int bc_lo[3], bc_hi[3];
+    int mthlim, order, tw, ctrl_mode;
+    long long npos;  // edge-box positions (n0 + 3)(n1 + 3)(n2 + 3)
+};
+
+// Constant-coefficient acoustics, q = (p, u, v, w); the velocity along axis
+// a is q[1 + a] (upstream riemann rpn3/rpt3/rptt3_acoustics.f90).
+template <typename T>
+struct Rp3Acoustics {
+    static constexpr int M = 4, MW = 2;
+    struct Params {
+        T cc, zz;
+    };
+    static Params make(const double *pd) { return Params{(T)pd[2], (T)pd[3]}; }
+
+    template <int D>
+    __device__ __forceinline__ static void rpn3(const Params &P, const T *ql, const T *qr, T *W,
+                                                T *s, T *am, T *ap) {
+        constexpr int mn = 1 + D;
+        const T cc = P.cc, zz = P.zz;
+        const T d0 = qr[0] - ql[0];
+        const T d1 = qr[mn] - ql[mn];
+        const T a1 = (-d0 + zz * d1) / ((T)2 * zz);
+        const T a2 = (d0 + zz * d1) / ((T)2 * zz);
+#pragma unroll
+        for (int k = 0; k < 8; k++) W[k] = (T)0;
+        W[0] = -a1 * zz; W[mn] = a1;
+        s[0] = -cc;
+        W[4] = a2 * zz; W[4 + mn] = a2;
+        s[1] = cc;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            am[k] = s[0] * W[k];
+            ap[k] = s[1] * W[4 + k];
+        }
+    }
+
+    // split asdq along axis t into the parts moving down (bm) and up (bp)
+    template <int TA>
+    __device__ __forceinline__ static void rpt3(const Params &P, const T *asdq, T *bm, T *bp) {
+        constexpr int mt = 1 + TA;
+        const T cc = P.cc, zz = P.zz;
+        const T a1 = (-asdq[0] + zz * asdq[mt]) / ((T)2 * zz);
+        const T a2 = (asdq[0] + zz * asdq[mt]) / ((T)2 * zz);
+#pragma unroll
+        for (int k = 0; k < 4; k++) bm[k] = bp[k] = (T)0;
+        bm[0] = cc * a1 * zz; bm[mt] = -cc * a1;
+        bp[0] = cc * a2 * zz; bp[mt] = cc * a2;
+    }
+
+    // split a fluctuation already split along T1 along T2 (constant
+    // coefficients: the split along T2 does not depend on the state)
+    template <int T1, int T2>
+    __device__ __forceinline__ static void rptt3(const Params &P, const T *b, T *cm, T *cp) {
+        rpt3<T2>(P, b, cm, cp);
+    }
+};
+
+// Field planes of the workspace (doubles), per edge position.
+template <class RP>
+struct Fields {
+    static constexpr int M = RP::M, MW = RP::MW;
+    static constexpr int W = 0, S = MW * M, AM = S + MW, AP = AM + M, FA = AP + M;
+    static constexpr int AMC = FA + M, APC = AMC + 12 * M, NF = APC + 12 * M;
+    // chain entry (G: part 0, H: part 1; face s 0/1; t-offset o 0..2)
+    __host__ __device__ static constexpr int ce(int part, int s, int o, int k) {
+        return part * 6 * M + (s * 3 + o) * M + k;
+    }
+};
+
+// Box position of (x, y, z), each in [-1, n + 1].
+__device__ __forceinline__ long long bpos(const Args3 &a, int x, int y, int z) {
+    return (long long)(x + 1) +
+           (long long)(a.n[0] + 3) * ((long long)(y + 1) + (long long)(a.n[1] + 3) * (z + 1));
+}
+
+// q(k) at cell (g0, g1, g2), each in [-2, n+1], through the boundary
+// conditions (x, then y, then z, as the ghost fill composes them; a wall
+// negates the velocity normal to it).
+template <int M>
+__device__ __forceinline__ double load_q3(const Args3 &a, const double *__restrict__ q, int k,
+                                          int g0, int g1, int g2) {
+    int g[3] = {g0, g1, g2}, si[3];
+    bool neg = false;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int n = a.n[d];
+        int v = min(max(g[d], -2), n + 1);
+        if (v < 0) {
+            const int b = a.bc_lo[d];
+            if (b == GCLAW_BC_EXTRAP) v = 0;
+            else if (b == GCLAW_BC_PERIODIC) v = v + n;
+            else { v = -1 - v; neg = neg || (M > 1 && k == 1 + d); }
+        } else if (v >= n) {
+            const int b = a.bc_hi[d];
+            if (b == GCLAW_BC_EXTRAP) v = n - 1;
+            else if (b == GCLAW_BC_PERIODIC) v = v - n;
+            else { v = 2 * n - 1 - v; neg = neg || (M > 1 && k == 1 + d); }
+        }
+        si[d] = v;
+    }
+    const double x = __ldg(q + k + (size_t)M * ((size_t)si[0] + (size_t)a.n[0] *
+                                                 ((size_t)si[1] + (size_t)a.n[1] * (size_t)si[2])));
+    return __longlong_as_double(__double_as_longlong(x) ^
+                                (neg ? (long long)0x8000000000000000ull : 0ll));
+}
+
+// dt, parity and skip flag of this launch (device time-step control).
+struct Launch {
+    double dt;
+    int par, skip;
+};
+__device__ __forceinline__ Launch launch_state(const Args3 &a) {
+    __shared__ double s_dt;
+    __shared__ int s_par, s_skip;
+    if (threadIdx.x == 0) {
+        if (a.ctrl_mode) {
+            const volatile gclaw_ctrl *c = a.ctrl;
+            s_skip = c->done;
+            s_dt = c->dt;
+            s_par = c->parity;
+        } else {
+            s_skip = 0;
+            s_dt = a.dt;
+            s_par = 0;
+        }
+    }
+    __syncthreads();
+    return Launch{s_dt, s_par, s_skip};
+}
+
+// ---- k_edges: normal Riemann problems ---------------------------------------
+template <template <typename> class RPT, int D>
+__global__ void __launch_bounds__(NT3) k_edges(const Args3 a,
+                                               const typename RPT<double>::Params P) {
+    using RP = RPT<double>;
+    using F = Fields<RP>;
+    constexpr int M = RP::M, MW = RP::MW;
+    constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+    const Launch L = launch_state(a);
+    if (L.skip) return;
+    const double *__restrict__ qin = a.qin[L.par];
+    const double dtdn = L.dt / a.d[D];
+    double cmax = 0.0;
+    bool bad = false;
+    const long long idx = (long long)blockIdx.x * NT3 + threadIdx.x;
+    if (idx < a.npos) {
+        const int X = a.n[0] + 3, Y = a.n[1] + 3;
+        int p[3];
+        p[0] = (int)(idx % X) - 1;
+        p[1] = (int)((idx / X) % Y) - 1;
+        p[2] = (int)(idx / ((long long)X * Y)) - 1;
+        int l[3] = {p[0], p[1], p[2]};
+        l[D] -= 1;
+        double ql[M], qr[M];
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            ql[k] = load_q3<M>(a, qin, k, l[0], l[1], l[2]);
+            qr[k] = load_q3<M>(a, qin, k, p[0], p[1], p[2]);
+        }
+        double W[MW * M], s[MW], am[M], ap[M];
+        RP::template rpn3<D>(P, ql, qr, W, s, am, ap);
+        double *ws = a.ws;
+        const long long np = a.npos;
+#pragma unroll
+        for (int f = 0; f < MW * M; f++) ws[(F::W + f) * np + idx] = W[f];
+#pragma unroll
+        for (int q = 0; q < MW; q++) ws[(F::S + q) * np + idx] = s[q];
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            ws[(F::AM + k) * np + idx] = am[k];
+            ws[(F::AP + k) * np + idx] = ap[k];
+        }
+        // Courant numbers of the edges 0..n along the sweep in every slice
+        // (ghost slices included, as the serial sweep counts them)
+        if (p[D] >= 0 && p[D] <= a.n[D] && p[T1] <= a.n[T1] && p[T2] <= a.n[T2]) {
+#pragma unroll
+            for (int q = 0; q < MW; q++) {
+                bad |= isnan_v(s[q]);
+                cmax = max_abs(cmax, dtdn * s[q]);
+            }
+        }
+    }
+    // block max and flag, then one atomic each
+    __shared__ double s_red[NT3 / 32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) cmax = fmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = cmax;
+    const int any = __syncthreads_or(bad ? 1 : 0);
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < NT3 / 32; w++) cmax = fmax(cmax, s_red[w]);
+        if (cmax > 0.0)
+            atomicMax(&a.ctrl->smax_bits[0], (unsigned long long)__double_as_longlong(cmax));
+        if (any) atomicOr(&a.ctrl->flags, 1u);
+    }
+}
+
+// ---- k_chains: limiter, correction flux, transverse chains -----------------
+template <class RP, int D>
+__device__ __forceinline__ void chain(const typename RP::Params &P, const double *asdq,
+                                      bool dbl, double h, double f1, double f2, double *ws,
+                                      long long np, long long idx, int base) {
+    using F = Fields<RP>;
+    constexpr int M = RP::M;
+    constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+    double bm[M], bp[M], cm[M], cp[M];
+    RP::template rpt3<T1>(P, asdq, bm, bp);
+    RP::template rpt3<T2>(P, asdq, cm, cp);
+    double g[2][3][M], hh[2][3][M];
+#pragma unroll
+    for (int s = 0; s < 2; s++)
+#pragma unroll
+        for (int o = 0; o < 3; o++)
+#pragma unroll
+            for (int k = 0; k < M; k++) g[s][o][k] = hh[s][o][k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        g[0][1][k] = 0.0 - h * bm[k];
+        g[1][1][k] = 0.0 - h * bp[k];
+        hh[0][1][k] = 0.0 - h * cm[k];
+        hh[1][1][k] = 0.0 - h * cp[k];
+    }
+    if (dbl) {
+        double cmb[M], cpb[M];
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+            RP::template rptt3<T1, T2>(P, s ? bp : bm, cmb, cpb);
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                g[s][1][k] = g[s][1][k] + f2 * (cpb[k] - cmb[k]);
+                g[s][2][k] = 0.0 - f2 * cpb[k];
+                g[s][0][k] = 0.0 + f2 * cmb[k];
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+            RP::template rptt3<T2, T1>(P, s ? cp : cm, cmb, cpb);
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                hh[s][1][k] = hh[s][1][k] + f1 * (cpb[k] - cmb[k]);
+                hh[s][2][k] = 0.0 - f1 * cpb[k];
+                hh[s][0][k] = 0.0 + f1 * cmb[k];
+            }
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < 2; s++)
+#pragma unroll
+        for (int o = 0; o < 3; o++)
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                ws[(long long)(base + F::ce(0, s, o, k)) * np + idx] = g[s][o][k];
+                ws[(long long)(base + F::ce(1, s, o, k)) * np + idx] = hh[s][o][k];
+            }
+}
+
+template <template <typename> class RPT, int D>
+__global__ void __launch_bounds__(NT3) k_chains(const Args3 a,
+                                                const typename RPT<double>::Params P) {
+    using RP = RPT<double>;
+    using F = Fields<RP>;
+    constexpr int M = RP::M, MW = RP::MW;
+    constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+    const Launch L = launch_state(a);
+    if (L.skip) return;
+    const long long idx = (long long)blockIdx.x * NT3 + threadIdx.x;
+    if (idx >= a.npos) return;
+    const int X = a.n[0] + 3, Y = a.n[1] + 3;
+    int p[3];
+    p[0] = (int)(idx % X) - 1;
+    p[1] = (int)((idx / X) % Y) - 1;
+    p[2] = (int)(idx / ((long long)X * Y)) - 1;
+    // edges 0..n along the sweep, slices -1..n across it
+    if (p[D] < 0 || p[D] > a.n[D] || p[T1] > a.n[T1] || p[T2] > a.n[T2]) return;
+    double *ws = a.ws;
+    const long long np = a.npos;
+    long long stepd = 1;
+    if (D >= 1) stepd *= X;
+    if (D >= 2) stepd *= Y;
+    const double dtdn = L.dt / a.d[D], dtt1 = L.dt / a.d[T1], dtt2 = L.dt / a.d[T2];
+
+    double W[MW * M], s[MW], cq[M];
+#pragma unroll
+    for (int f = 0; f < MW * M; f++) W[f] = ws[(F::W + f) * np + idx];
+#pragma unroll
+    for (int q = 0; q < MW; q++) s[q] = ws[(F::S + q) * np + idx];
+#pragma unroll
+    for (int k = 0; k < M; k++) cq[k] = 0.0;
+    if (a.order == 2) {
+#pragma unroll
+        for (int q = 0; q < MW; q++) {
+            const int lim = (a.mthlim >> (8 * q)) & 0xff;
+            if (lim == 0) continue;
+            double wn2 = 0.0;
+#pragma unroll
+            for (int k = 0; k < M; k++) wn2 = wn2 + W[q * M + k] * W[q * M + k];
+            if (eq0(wn2)) continue;
+            double dot = 0.0;
+            if (gt0(s[q])) {  // upwind: the edge before
+#pragma unroll
+                for (int k = 0; k < M; k++)
+                    dot = dot + ws[(F::W + q * M + k) * np + idx - stepd] * W[q * M + k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < M; k++)
+                    dot = dot + W[q * M + k] * ws[(F::W + q * M + k) * np + idx + stepd];
+            }
+            double phi = 0.0;
+            if (!le0(dot)) {
+                const double th = dot / wn2;
+                phi = gt0(th) ? philim_pos<double>(lim, th) : philim<double>(lim, th);
+            }
+#pragma unroll
+            for (int k = 0; k < M; k++) W[q * M + k] = phi * W[q * M + k];
+        }
+        const double dtave = 0.5 * (dtdn + dtdn);
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            double c = 0.0;
+#pragma unroll
+            for (int q = 0; q < MW; q++) {
+                const double sa = fabs(s[q]);
+                c = c + sa * (1.0 - sa * dtave) * W[q * M + k];
+            }
+            cq[k] = c;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < M; k++) ws[(F::FA + k) * np + idx] = 0.0 + 0.5 * cq[k];
+
+    const int single = a.tw / 10;
+    const bool dbl = (a.tw % 10) > 0;
+    double am[M], ap[M];
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        am[k] = ws[(F::AM + k) * np + idx];
+        ap[k] = ws[(F::AP + k) * np + idx];
+        if (a.order == 2 && single == 2) {
+            am[k] = am[k] + cq[k];
+            ap[k] = ap[k] - cq[k];
+        }
+    }
+    if (single > 0) {
+        const double h = 0.5 * dtdn;
+        const double sixth = 1.0 / 6.0;
+        const double f1 = sixth * dtdn * dtt1, f2 = sixth * dtdn * dtt2;
+        chain<RP, D>(P, am, dbl, h, f1, f2, ws, np, idx, F::AMC);
+        chain<RP, D>(P, ap, dbl, h, f1, f2, ws, np, idx, F::APC);
+    } else {
+#pragma unroll
+        for (int e = 0; e < 12 * M; e++) {
+            ws[(long long)(F::AMC + e) * np + idx] = 0.0;
+            ws[(long long)(F::APC + e) * np + idx] = 0.0;
+        }
+    }
+}
+
+// ---- k_update: per-cell accumulation of one sweep ---------------------------
+template <template <typename> class RPT, int D>
+__global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
+    using RP = RPT<double>;
+    using F = Fields<RP>;
+    constexpr int M = RP::M;
+    constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+    const Launch L = launch_state(a);
+    if (L.skip) return;
+    const long long ncell = (long long)a.n[0] * a.n[1] * a.n[2];
+    const long long cid = (long long)blockIdx.x * NT3 + threadIdx.x;
+    if (cid < ncell) {
+        int p[3];
+        p[0] = (int)(cid % a.n[0]);
+        p[1] = (int)((cid / a.n[0]) % a.n[1]);
+        p[2] = (int)(cid / ((long long)a.n[0] * a.n[1]));
+        // the x-sweep starts from the old state, the others add to the new one
+        const double *src = D == 0 ? a.qin[L.par] : a.qout[L.par];
+        double *dst = a.qout[L.par];
+        const size_t o = (size_t)M * (size_t)cid;
+        const double *ws = a.ws;
+        const long long np = a.npos;
+        const double dtn = L.dt / a.d[D], dt1 = L.dt / a.d[T1], dt2 = L.dt / a.d[T2];
+        double v[M];
+#pragma unroll
+        for (int k = 0; k < M; k++) v[k] = src[o + k];
+        const int c = p[D], A = p[T1], B = p[T2];
+        for (int db = -1; db <= 1; db++)
+            for (int da = -1; da <= 1; da++) {
+                int e0[3];
+                e0[D] = c; e0[T1] = A - da; e0[T2] = B - db;
+                int e1[3] = {e0[0], e0[1], e0[2]};
+                e1[D] = c + 1;
+                const long long i0 = bpos(a, e0[0], e0[1], e0[2]);
+                const long long i1 = bpos(a, e1[0], e1[1], e1[2]);
+                // flux entry (part, face s, offset o) of this slice at cell c
+                auto ent = [&](int part, int s, int off, int k) {
+                    const double am = ws[(long long)(F::AMC + F::ce(part, s, off + 1, k)) * np + i1];
+                    const double ap = ws[(long long)(F::APC + F::ce(part, s, off + 1, k)) * np + i0];
+                    return (0.0 + am) + ap;
+                };
+#pragma unroll
+                for (int k = 0; k < M; k++) {
+                    if (da == 0 && db == 0) {
+                        const double qa = (0.0 - dtn * ws[(F::AP + k) * np + i0]) -
+                                          dtn * ws[(F::AM + k) * np + i1];
+                        const double fa0 = ws[(F::FA + k) * np + i0];
+                        const double fa1 = ws[(F::FA + k) * np + i1];
+                        v[k] = v[k] + qa - dtn * (fa1 - fa0) -
+                               dt1 * (ent(0, 1, 0, k) - ent(0, 0, 0, k)) -
+                               dt2 * (ent(1, 1, 0, k) - ent(1, 0, 0, k));
+                    } else {
+                        const double gt = da == 0 ? 0.0 - dt1 * (ent(0, 1, db, k) - ent(0, 0, db, k))
+                                          : da == 1 ? dt1 * ent(0, 1, db, k)
+                                                    : 0.0 - dt1 * ent(0, 0, db, k);
+                        const double ht = db == 0 ? 0.0 - dt2 * (ent(1, 1, da, k) - ent(1, 0, da, k))
+                                          : db == 1 ? dt2 * ent(1, 1, da, k)
+                                                    : 0.0 - dt2 * ent(1, 0, da, k);
+                        v[k] = v[k] + gt + ht;
+                    }
+                }
+            }
+#pragma unroll
+        for (int k = 0; k < M; k++) dst[o + k] = v[k];
+    }
+    if (D == 2) {
+        // last block of the step: Courant number and evolve_to_time rules
+        // (the edges reduced Courant numbers themselves, so no dt/dx factor)
+        __shared__ int s_last;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            s_last = atomicAdd(&a.ctrl->blocks_done, 1u) == gridDim.x - 1;
+        }
+        __syncthreads();
+        if (s_last && threadIdx.x == 0) {
+            __threadfence();
+            finish_step(a.ctrl, a.ctrl_mode, L.dt, 1.0, 1.0);
+        }
+    }
+}
+
+template <template <typename> class RPT, int D>
+static int sweep(const gclaw3_solver *s, const Args3 &a, cudaStream_t st) {
+    const typename RPT<double>::Params P = RPT<double>::make(s->problem_data);
+    const unsigned nb = (unsigned)((a.npos + NT3 - 1) / NT3);
+    const long long ncell = (long long)s->mx * s->my * s->mz;
+    const unsigned nc = (unsigned)((ncell + NT3 - 1) / NT3);
+    k_edges<RPT, D><<<nb, NT3, 0, st>>>(a, P);
+    k_chains<RPT, D><<<nb, NT3, 0, st>>>(a, P);
+    k_update<RPT, D><<<nc, NT3, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
+}
+
+template <template <typename> class RPT>
+static int step_all(const gclaw3_solver *s, const Args3 &a, cudaStream_t st, int nsteps) {
+    for (int n = 0; n < nsteps; n++) {
+        int rc = sweep<RPT, 0>(s, a, st);
+        if (!rc) rc = sweep<RPT, 1>(s, a, st);
+        if (!rc) rc = sweep<RPT, 2>(s, a, st);
+        if (rc) return rc;
+    }
+    return GCLAW_OK;
+}
+
+static long long box_positions(const gclaw3_solver *s) {
+    return (long long)(s->mx + 3) * (long long)(s->my + 3) * (long long)(s->mz + 3);
+}
+
+static void fill_args(const gclaw3_solver *s, Args3 &a) {
+    a.d[0] = s->dx;
+    a.d[1] = s->dy;
+    a.d[2] = s->dz;
+    a.n[0] = s->mx;
+    a.n[1] = s->my;
+    a.n[2] = s->mz;
+    for (int d = 0; d < 3; d++) {
+        a.bc_lo[d] = s->bc_lower[d];
+        a.bc_hi[d] = s->bc_upper[d];
+    }
+    a.mthlim = 0;
+    for (int p = 0; p < 4; p++) a.mthlim |= (s->mthlim[p] & 0xff) << (8 * p);
+    a.order = s->order;
+    a.tw = s->transverse_waves;
+    a.npos = box_positions(s);
+}
+
+}  // namespace g3
+}  // namespace gclaw
+
+using namespace gclaw;
+using namespace gclaw::g3;
+
+extern "C" {
+
+int gclaw3_rp_shape(int rp, int *num_eqn, int *num_waves) {
+    switch (rp) {
+    case GCLAW3_RP_ACOUSTICS_3D: *num_eqn = 4; *num_waves = 2; return GCLAW_OK;
+    default: return GCLAW_ERR_ARG;
+    }
+}
+
+int gclaw3_check(const gclaw3_solver *s) {
+    int m, mw;
+    if (!s || gclaw3_rp_shape(s->rp, &m, &mw)) return GCLAW_ERR_ARG;
+    if (s->mx < 2 || s->my < 2 || s->mz < 2) return GCLAW_ERR_ARG;
+    if (!(s->dx > 0.0) || !(s->dy > 0.0) || !(s->dz > 0.0)) return GCLAW_ERR_ARG;
+    if ((double)(s->mx + 3) * (s->my + 3) * (s->mz + 3) > 4.0e9) return GCLAW_ERR_ARG;
+    for (int d = 0; d < 3; d++) {
+        if (s->bc_lower[d] == GCLAW_BC_CUSTOM || s->bc_upper[d] == GCLAW_BC_CUSTOM)
+            return GCLAW_ERR_UNSUPPORTED;
+        if (s->bc_lower[d] < GCLAW_BC_EXTRAP || s->bc_lower[d] > GCLAW_BC_WALL ||
+            s->bc_upper[d] < GCLAW_BC_EXTRAP || s->bc_upper[d] > GCLAW_BC_WALL)
+            return GCLAW_ERR_ARG;
+        if ((s->bc_lower[d] == GCLAW_BC_PERIODIC) != (s->bc_upper[d] == GCLAW_BC_PERIODIC))
+            return GCLAW_ERR_ARG;
+    }
+    for (int p = 0; p < GCLAW_MAX_WAVES; p++)
+        if (s->mthlim[p] < 0 || s->mthlim[p] > 4) return GCLAW_ERR_UNSUPPORTED;
+    if (s->order < 1 || s->order > 2) return GCLAW_ERR_ARG;
+    const int tw = s->transverse_waves;
+    if (tw != 0 && tw != 10 && tw != 11 && tw != 20 && tw != 22) return GCLAW_ERR_UNSUPPORTED;
+    if (s->precision != GCLAW_PREC_FP64) return GCLAW_ERR_UNSUPPORTED;
+    if (!(s->problem_data[2] > 0.0) || !(s->problem_data[3] > 0.0)) return GCLAW_ERR_ARG;
+    return GCLAW_OK;
+}
+
+size_t gclaw3_workspace_bytes(const gclaw3_solver *s) {
+    if (gclaw3_check(s)) return 0;
+    return sizeof(double) * (size_t)Fields<Rp3Acoustics<double>>::NF * (size_t)box_positions(s);
+}
+
+int gclaw3_step(const gclaw3_solver *s, const double *q_dev, double *qnew_dev, double dt,
+                void *ws_dev, gclaw_ctrl *ctrl_dev, void *stream) {
+    int rc = gclaw3_check(s);
+    if (rc) return rc;
+    if (!q_dev || !qnew_dev || q_dev == qnew_dev || !ws_dev || !ctrl_dev || !(dt > 0.0))
+        return GCLAW_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(ctrl_dev, 0, sizeof(gclaw_ctrl), st) != cudaSuccess)
+        return GCLAW_ERR_CUDA;
+    Args3 a{};
+    fill_args(s, a);
+    a.qin[0] = a.qin[1] = q_dev;
+    a.qout[0] = a.qout[1] = qnew_dev;
+    a.ctrl = ctrl_dev;
+    a.ws = (double *)ws_dev;
+    a.dt = dt;
+    a.ctrl_mode = 0;
+    return step_all<Rp3Acoustics>(s, a, st, 1);
+}
+
+int gclaw3_advance(const gclaw3_solver *s, double *q0_dev, double *q1_dev, void *ws_dev,
+                   gclaw_ctrl *ctrl_dev, int nsteps, void *stream) {
+    int rc = gclaw3_check(s);
+    if (rc) return rc;
+    if (!q0_dev || !q1_dev || q0_dev == q1_dev || !ws_dev || !ctrl_dev || nsteps < 0)
+        return GCLAW_ERR_ARG;
+    Args3 a{};
+    fill_args(s, a);
+    a.qin[0] = q0_dev;
+    a.qin[1] = q1_dev;
+    a.qout[0] = q1_dev;
+    a.qout[1] = q0_dev;
+    a.ctrl = ctrl_dev;
+    a.ws = (double *)ws_dev;
+    a.dt = 0.0;
+    a.ctrl_mode = 1;
+    return step_all<Rp3Acoustics>(s, a, (cudaStream_t)stream, nsteps);
+}
+
+}  // extern "C"

@@ -155,3 +155,76 @@ class DeviceProblem:
             c = self.read_ctrl(stream)
             if c.done:
                 return c
+
+
+def make_solver3_struct(rp_id, mx, my, mz, dx, dy, dz, bc_lower, bc_upper, mthlim, order, tw,
+                        precision, problem_data):
+    """The gclaw3_solver C struct (include/gclaw3.h)."""
+    s = _lib.GclawSolver3()
+    s.rp = int(rp_id)
+    s.mx, s.my, s.mz = int(mx), int(my), int(mz)
+    s.dx, s.dy, s.dz = float(dx), float(dy), float(dz)
+    for d in range(3):
+        s.bc_lower[d] = int(bc_lower[d])
+        s.bc_upper[d] = int(bc_upper[d])
+    lim = list(mthlim) + [0] * (_lib.MAX_WAVES - len(mthlim))
+    for p in range(_lib.MAX_WAVES):
+        s.mthlim[p] = int(lim[p])
+    s.order = int(order)
+    s.transverse_waves = int(tw)
+    s.precision = int(precision)
+    pd = list(problem_data) + [0.0] * (8 - len(problem_data))
+    for i in range(8):
+        s.problem_data[i] = float(pd[i])
+    return s
+
+
+class DeviceProblem3(DeviceProblem):
+    """The 3D counterpart: two (num_eqn, mx, my, mz) state buffers, the step's
+    workspace and a control block on one CUDA device (gclaw3_step /
+    gclaw3_advance); time-step control as in 2D."""
+
+    def __init__(self, solver_struct, device=None, strict=False):
+        self.s = solver_struct
+        self.L = L = _lib.lib(strict)
+        self.device = torch.device(device or "cuda")
+        self.split = False
+        self.aux = None
+        _lib.check(L.gclaw3_check(ctypes.byref(self.s)), "gclaw3_check")
+        m, mw = ctypes.c_int(), ctypes.c_int()
+        _lib.check(L.gclaw3_rp_shape(self.s.rp, ctypes.byref(m), ctypes.byref(mw)))
+        self.m, self.mw = m.value, mw.value
+        self.mx, self.my, self.mz = self.s.mx, self.s.my, self.s.mz
+        shape = (self.mz, self.my, self.mx, self.m)
+        self.q = [torch.empty(shape, dtype=torch.float64, device=self.device),
+                  torch.empty(shape, dtype=torch.float64, device=self.device)]
+        nbytes = L.gclaw3_workspace_bytes(ctypes.byref(self.s))
+        self.ws = torch.empty(int(nbytes), dtype=torch.uint8, device=self.device)
+        self.ctrl = torch.zeros(256, dtype=torch.uint8, device=self.device)
+        self._ctrl_host = torch.empty(256, dtype=torch.uint8, pin_memory=True)
+        self.ctrl_init(0.0, 1.0, 0.0)
+
+    def upload(self, q, buf=0):
+        """Copy a host (num_eqn, mx, my, mz) array into state buffer ``buf``."""
+        qf = np.asfortranarray(q, dtype=np.float64)
+        if qf.shape != (self.m, self.mx, self.my, self.mz):
+            raise ValueError(f"q has shape {qf.shape}, expected "
+                             f"{(self.m, self.mx, self.my, self.mz)}")
+        self.q[buf].copy_(torch.from_numpy(qf.T))
+
+    def download(self, buf=0):
+        return np.asfortranarray(self.q[buf].cpu().numpy().T)
+
+    def advance(self, nlaunch, stream=None):
+        _lib.check(self.L.gclaw3_advance(
+            ctypes.byref(self.s), ctypes.c_void_p(self.q[0].data_ptr()),
+            ctypes.c_void_p(self.q[1].data_ptr()), ctypes.c_void_p(self.ws.data_ptr()),
+            ctypes.c_void_p(self.ctrl.data_ptr()), int(nlaunch), _stream_handle(stream)),
+            "gclaw3_advance")
+
+    def step(self, dt, src=0, stream=None):
+        _lib.check(self.L.gclaw3_step(
+            ctypes.byref(self.s), ctypes.c_void_p(self.q[src].data_ptr()),
+            ctypes.c_void_p(self.q[1 - src].data_ptr()), float(dt),
+            ctypes.c_void_p(self.ws.data_ptr()), ctypes.c_void_p(self.ctrl.data_ptr()),
+            _stream_handle(stream)), "gclaw3_step")

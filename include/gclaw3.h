@@ -1,0 +1,71 @@
+/*
+ * gclaw3.h -- C ABI of the classic unsplit 3D wave-propagation step on GB300.
+ *
+ * Replaces PyClaw's f2py call classic3.step3(...) for ClawSolver3D
+ * (upstream pyclaw/src/pyclaw/classic/solver.py, step3.f90, flux3.f90;
+ * empty submodules in the mounted clawpack 5.14.0 tree, meson.build:62-76)
+ * with the Langseth-LeVeque method: per direction, normal Riemann solves,
+ * limited correction fluxes, transverse splitting of the fluctuations in
+ * both transverse directions and, with transverse_waves 11 or 22, the
+ * corner (double transverse) terms.
+ *
+ * Arrays follow the f2py convention: q is (num_eqn, mx, my, mz) Fortran
+ * order (component fastest).  The library allocates nothing: the caller
+ * passes a device workspace of gclaw3_workspace_bytes() bytes and a
+ * gclaw_ctrl block (include/gclaw.h), which also carries the time-step
+ * control of gclaw3_advance.
+ */
+#ifndef GCLAW3_H
+#define GCLAW3_H
+
+#include <stddef.h>
+
+#include "gclaw.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* acoustics_3D: m = 4 (p, u, v, w), 2 waves; pd: rho, bulk, cc, zz */
+#define GCLAW3_RP_ACOUSTICS_3D 1
+
+typedef struct gclaw3_solver {
+    int rp;                       /* GCLAW3_RP_* */
+    int mx, my, mz;               /* interior cells, each >= 2 */
+    double dx, dy, dz;
+    int bc_lower[3], bc_upper[3]; /* GCLAW_BC_EXTRAP / PERIODIC / WALL per axis */
+    int mthlim[GCLAW_MAX_WAVES];  /* limiter per wave family */
+    int order;                    /* 1 or 2 */
+    int transverse_waves;         /* 0, 10, 11, 20 or 22 (ClawSolver3D: 22) */
+    int precision;                /* GCLAW_PREC_FP64 */
+    double problem_data[8];
+} gclaw3_solver;
+
+int gclaw3_rp_shape(int rp, int *num_eqn, int *num_waves);
+
+/* 0 if the description can be stepped, else GCLAW_ERR_ARG or
+ * GCLAW_ERR_UNSUPPORTED (FP32, unknown transverse option). */
+int gclaw3_check(const gclaw3_solver *s);
+
+/* Bytes of device workspace a step of this grid needs. */
+size_t gclaw3_workspace_bytes(const gclaw3_solver *s);
+
+/* One step of size dt from q_dev into qnew_dev (interior arrays, distinct).
+ * ctrl_dev receives the Courant number (cfl) and status (GCLAW_OK or
+ * GCLAW_NONPHYSICAL); only its reduction fields are used.  Asynchronous on
+ * stream. */
+int gclaw3_step(const gclaw3_solver *s, const double *q_dev, double *qnew_dev, double dt,
+                void *ws_dev, gclaw_ctrl *ctrl_dev, void *stream);
+
+/* nsteps attempts under device time-step control (gclaw_ctrl_init first):
+ * the state ping-pongs between q0_dev and q1_dev, ctrl->parity names the
+ * accepted one; rejected attempts and finished runs are skipped on the
+ * device.  Capturable in a CUDA graph. */
+int gclaw3_advance(const gclaw3_solver *s, double *q0_dev, double *q1_dev, void *ws_dev,
+                   gclaw_ctrl *ctrl_dev, int nsteps, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

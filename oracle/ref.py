@@ -276,3 +276,72 @@ def evolve(step_fn, q, t, tend, dt, *, cfl_max=1.0, cfl_desired=0.9, dt_max=1e99
         if max_accepted is None and t < tend:
             raise RuntimeError("Maximum number of timesteps have been taken")
     return q, t, dt, st
+
+
+# ---------------------------------------------------------------------------
+# 3D (classic3_ref.c): the unsplit 3D step.  q arrays are (m, mx, my, mz).
+# ---------------------------------------------------------------------------
+LIB3 = os.path.join(HERE, "libclassic3_ref.so")
+RP3_ACOUSTICS, RP3_ADVECTION = 1, 100
+SHAPES3 = {RP3_ACOUSTICS: (4, 2), RP3_ADVECTION: (1, 1)}
+_lib3 = None
+
+
+def lib3():
+    global _lib3
+    if _lib3 is None:
+        if not os.path.exists(LIB3):
+            build()
+        L = ctypes.CDLL(LIB3)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        i, d = ctypes.c_int, ctypes.c_double
+        L.gclaw3_ref_fill_ghosts.argtypes = [i, i, i, i, i, ip, ip, dp, dp]
+        L.gclaw3_ref_step3.argtypes = [i, dp, i, i, i, dp, dp, d, d, d, d, i, i, ip, dp, i]
+        L.gclaw3_ref_step.argtypes = [i, dp, i, i, i, dp, dp, d, d, d, d, i, i, ip, ip, ip, dp, i]
+        _lib3 = L
+    return _lib3
+
+
+def fill_ghosts3(q, bc_lower, bc_upper):
+    m, mx, my, mz = q.shape
+    qf = np.asfortranarray(q, dtype=np.float64)
+    qbc = np.zeros((m, mx + 4, my + 4, mz + 4), order="F")
+    rc = lib3().gclaw3_ref_fill_ghosts(m, mx, my, mz, 2, _ip(np.array(bc_lower, np.int32)),
+                                       _ip(np.array(bc_upper, np.int32)), _dp(qf), _dp(qbc))
+    if rc:
+        raise ValueError(f"gclaw3_ref_fill_ghosts failed: {rc}")
+    return qbc
+
+
+def step3(rp, pd, q, dx, dy, dz, dt, bc_lower, bc_upper, order=2, tw=22, mthlim=(4,) * 4,
+          nthreads=1):
+    """Ghost fill + unsplit 3D step; returns (qnew, cfl)."""
+    m, mx, my, mz = q.shape
+    qf = np.asfortranarray(q, dtype=np.float64)
+    qout = np.zeros_like(qf, order="F")
+    cfl = np.zeros(1)
+    lim = np.zeros(5, np.int32)
+    lim[:len(mthlim)] = mthlim
+    rc = lib3().gclaw3_ref_step(rp, _dp(_pd(pd)), mx, my, mz, _dp(qf), _dp(qout), dx, dy, dz,
+                                dt, order, tw, _ip(lim), _ip(np.array(bc_lower, np.int32)),
+                                _ip(np.array(bc_upper, np.int32)), _dp(cfl), nthreads)
+    if rc:
+        raise ValueError(f"gclaw3_ref_step failed: {rc}")
+    return qout, float(cfl[0])
+
+
+def step3_bc(rp, pd, qbc, dx, dy, dz, dt, order=2, tw=22, mthlim=(4,) * 4, nthreads=1):
+    """The 3D step on a ghost-filled (m, mx+4, my+4, mz+4) array."""
+    m = qbc.shape[0]
+    mx, my, mz = (s - 4 for s in qbc.shape[1:])
+    qf = np.asfortranarray(qbc, dtype=np.float64)
+    qout = np.zeros_like(qf, order="F")
+    cfl = np.zeros(1)
+    lim = np.zeros(5, np.int32)
+    lim[:len(mthlim)] = mthlim
+    rc = lib3().gclaw3_ref_step3(rp, _dp(_pd(pd)), mx, my, mz, _dp(qf), _dp(qout), dx, dy, dz,
+                                 dt, order, tw, _ip(lim), _dp(cfl), nthreads)
+    if rc:
+        raise ValueError(f"gclaw3_ref_step3 failed: {rc}")
+    return qout, float(cfl[0])

@@ -9,15 +9,18 @@ import pytest
 from clawpack_gb300 import _lib
 from clawpack_gb300.device import make_solver_struct
 
-HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
-                      "gclaw.h")
+INCLUDE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+HEADER = os.path.join(INCLUDE, "gclaw.h")
+HEADERS = [HEADER, os.path.join(INCLUDE, "gclaw3.h")]
 
 
 def declared_functions():
-    src = open(HEADER).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_]+\s*\*?\s*(gclaw_[a-z0-9_]+)\s*\(", src,
-                                 flags=re.M)))
+    names = set()
+    for h in HEADERS:
+        src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        names |= set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(gclaw3?_[a-z0-9_]+)\s*\(",
+                                src, flags=re.M))
+    return sorted(names)
 
 
 @pytest.mark.parametrize("strict", [False, True])
@@ -30,8 +33,8 @@ def test_exports_every_declared_symbol(strict):
     assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
 
 
-def _offsets_from_header(struct_name):
-    src = open(HEADER).read()
+def _offsets_from_header(struct_name, header=HEADER):
+    src = open(header).read()
     body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (struct_name, struct_name), src,
                      re.S).group(1)
     body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
@@ -53,6 +56,8 @@ def _offsets_from_header(struct_name):
 def test_struct_layouts_match_header():
     for cls, name in ((_lib.GclawSolver, "gclaw_solver"), (_lib.GclawCtrl, "gclaw_ctrl")):
         assert [f[0] for f in cls._fields_] == _offsets_from_header(name)
+    assert [f[0] for f in _lib.GclawSolver3._fields_] == _offsets_from_header(
+        "gclaw3_solver", HEADERS[1])
     assert ctypes.sizeof(_lib.GclawCtrl) == 144
     assert ctypes.sizeof(_lib.GclawCtrl) <= 256
 

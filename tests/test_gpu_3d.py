@@ -1,0 +1,109 @@
+"""The unsplit 3D step (gclaw3_step / gclaw3_advance, acoustics_3D) on the
+GPU against the oracle's restatement of classic3.
+
+The -fmad=false build must reproduce the oracle bit for bit for every
+transverse option (0, 10, 11, 20, 22), order, limiter and boundary mix,
+including grids of 2 cells in a direction; the product build stays within
+1e-13 per step; device-controlled time stepping follows the oracle's
+evolve_to_time within 1e-12; FP32 and unknown transverse options are
+refused."""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+from clawpack_gb300 import _lib
+from clawpack_gb300.device import DeviceProblem3, make_solver3_struct
+from tests.helpers import rel_l1
+
+pytestmark = pytest.mark.gpu
+PD3 = [1.0, 4.0, 2.0, 2.0]
+
+
+def gpu_step3(q, d, dt, bcl, bcu, order=2, tw=22, lim=4, strict=False):
+    m, mx, my, mz = q.shape
+    s = make_solver3_struct(1, mx, my, mz, *d, bcl, bcu, [lim] * 2, order, tw, 0, PD3)
+    dev = DeviceProblem3(s, strict=strict)
+    dev.upload(q)
+    dev.step(dt, src=0)
+    c = dev.read_ctrl()
+    return dev.download(1), c
+
+
+SIZES = [(2, 2, 2), (5, 4, 3), (17, 9, 12), (24, 20, 6)]
+BCS = [([1, 1, 1], [1, 1, 1]), ([2, 2, 2], [2, 2, 2]), ([3, 3, 3], [3, 3, 3]),
+       ([3, 1, 2], [1, 3, 2])]
+
+
+@pytest.mark.parametrize("shape", SIZES)
+@pytest.mark.parametrize("bcl,bcu", BCS)
+def test_strict_bitwise(cuda, oracle, shape, bcl, bcu):
+    rng = np.random.default_rng(sum(shape) + bcl[0])
+    q = np.asfortranarray(rng.normal(size=(4,) + shape))
+    d = (1.0 / shape[0], 1.1 / shape[1], 0.9 / shape[2])
+    dt = 0.1 * min(d) / 2.0
+    lim = [1, 2, 3, 4][sum(shape) % 4]
+    qo, cflo = oracle.step3(1, PD3, q, *d, dt, bcl, bcu, 2, 22, [lim] * 2)
+    qs, c = gpu_step3(q, d, dt, bcl, bcu, lim=lim, strict=True)
+    assert c.status == 0
+    assert np.array_equal(qs, qo), np.abs(qs - qo).max()
+    assert c.cfl == cflo
+    qp, cp = gpu_step3(q, d, dt, bcl, bcu, lim=lim)
+    assert rel_l1(qp, qo) <= 1e-13 and abs(cp.cfl - cflo) <= 1e-14 * cflo
+
+
+@pytest.mark.parametrize("order,tw,lim", [(2, 22, 4), (2, 20, 2), (2, 11, 3), (1, 10, 0),
+                                          (2, 0, 1), (1, 0, 0), (2, 22, 0)])
+def test_options_strict_bitwise(cuda, oracle, order, tw, lim):
+    rng = np.random.default_rng(order * 100 + tw + lim)
+    shape = (13, 11, 9)
+    q = np.asfortranarray(rng.normal(size=(4,) + shape))
+    d = (0.1, 0.12, 0.09)
+    dt = 0.02
+    bcl, bcu = [3, 1, 2], [1, 3, 2]
+    qo, cflo = oracle.step3(1, PD3, q, *d, dt, bcl, bcu, order, tw, [lim] * 2)
+    qs, c = gpu_step3(q, d, dt, bcl, bcu, order, tw, lim, strict=True)
+    assert np.array_equal(qs, qo)
+    assert c.cfl == cflo
+
+
+def test_device_controlled_evolve(cuda, oracle):
+    """A radial pressure pulse between walls: 0.3 time units under the
+    evolve_to_time rules on the device against the oracle's loop."""
+    mx, my, mz = 24, 20, 16
+    x = (np.arange(mx) + 0.5) / mx - 0.5
+    y = (np.arange(my) + 0.5) / my - 0.5
+    z = (np.arange(mz) + 0.5) / mz - 0.5
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    q = np.zeros((4, mx, my, mz), order="F")
+    q[0] = np.exp(-40.0 * (X ** 2 + Y ** 2 + Z ** 2))
+    d = (1.0 / mx, 1.0 / my, 1.0 / mz)
+    bc = [3, 3, 3]
+    s = make_solver3_struct(1, mx, my, mz, *d, bc, bc, [4, 4], 2, 22, 0, PD3)
+    dev = DeviceProblem3(s)
+    dev.upload(q)
+    c = dev.evolve(0.0, 0.002, 0.3, cfl_max=1.0, cfl_desired=0.9)
+    assert c.status == 0
+
+    def step(qq, dt):
+        return oracle.step3(1, PD3, qq, *d, dt, bc, bc, 2, 22, [4, 4], nthreads=8)
+
+    qo, t, dt, info = oracle.evolve(step, q, 0.0, 0.3, 0.002, cfl_desired=0.9, cfl_max=1.0)
+    assert c.numsteps == info["numsteps"]
+    assert rel_l1(dev.download(c.parity), qo) <= 1e-12
+    # acoustic energy stays bounded and the pulse spread out
+    assert np.abs(dev.download(c.parity)[0]).max() < 0.5
+
+
+def test_refusals(cuda):
+    L = _lib.lib()
+    s = make_solver3_struct(1, 8, 8, 8, 0.1, 0.1, 0.1, [1] * 3, [1] * 3, [4, 4], 2, 21, 0, PD3)
+    assert L.gclaw3_check(ctypes.byref(s)) == _lib.ERR_UNSUPPORTED
+    s.transverse_waves = 22
+    s.precision = 1
+    assert L.gclaw3_check(ctypes.byref(s)) == _lib.ERR_UNSUPPORTED
+    s.precision = 0
+    assert L.gclaw3_check(ctypes.byref(s)) == 0
+    s.mz = 1
+    assert L.gclaw3_check(ctypes.byref(s)) == _lib.ERR_ARG

@@ -1,0 +1,121 @@
+"""Known answers for the unsplit 3D step in the oracle (classic3_ref.c).
+
+Constant-velocity advection pins the transverse algebra: with order 1 and
+transverse_waves 11 the step is the corner transport upwind scheme, i.e.
+trilinear upwind interpolation, for every sign pattern of the velocity; with
+transverse_waves 0 it is donor cell.  Acoustics on data that do not vary in
+z reproduces the 2D step (the z-transverse and corner terms cancel); the
+step conserves every component with periodic boundaries, keeps a constant
+state bit for bit, commutes with a cyclic permutation of the axes, and
+reports c dt / min(dx, dy, dz) as its Courant number."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import ref
+from tests.helpers import rel_l1
+
+AC3, ADV3 = ref.RP3_ACOUSTICS, ref.RP3_ADVECTION
+PD3 = [1.0, 4.0, 2.0, 2.0]  # rho, bulk, c, Z
+
+
+def random3(m, shape, rng):
+    return np.asfortranarray(rng.normal(size=(m,) + shape))
+
+
+def trilinear(q, nu):
+    """Corner transport upwind: each cell takes the trilinear interpolation
+    of the upwind 2x2x2 block at its departure point (periodic)."""
+    out = np.zeros_like(q)
+    ax = []
+    for d, n in enumerate(nu):
+        s = 1 if n > 0 else -1
+        ax.append([(0, 1.0 - abs(n)), (s, abs(n))])
+    for sx, wx in ax[0]:
+        for sy, wy in ax[1]:
+            for sz, wz in ax[2]:
+                out += wx * wy * wz * np.roll(q, (sx, sy, sz), axis=(1, 2, 3))
+    return out
+
+
+@pytest.mark.parametrize("vel", [(1.0, 0.7, 0.4), (-0.8, 0.5, -0.3), (0.6, -0.9, 0.2),
+                                 (-0.5, -0.4, -0.7)])
+def test_advection_is_corner_transport_upwind(vel):
+    rng = np.random.default_rng(1)
+    shape = (9, 8, 7)
+    q = random3(1, shape, rng)
+    dt = 0.08
+    dx, dy, dz = 0.1, 0.12, 0.09
+    out, cfl = ref.step3(ADV3, list(vel), q, dx, dy, dz, dt, [2] * 3, [2] * 3, 1, 11, [0])
+    nu = (vel[0] * dt / dx, vel[1] * dt / dy, vel[2] * dt / dz)
+    assert np.allclose(out, trilinear(q, nu), rtol=0, atol=1e-14)
+    assert math.isclose(cfl, max(abs(n) for n in nu), rel_tol=1e-15)
+
+
+def test_advection_donor_cell():
+    rng = np.random.default_rng(2)
+    q = random3(1, (8, 9, 10), rng)
+    vel, dt, h = (0.9, -0.6, 0.3), 0.05, 0.1
+    out, _ = ref.step3(ADV3, list(vel), q, h, h, h, dt, [2] * 3, [2] * 3, 1, 0, [0])
+    expect = q.copy()
+    for d, v in enumerate(vel):
+        nu = v * dt / h
+        up = np.roll(q, 1 if v > 0 else -1, axis=d + 1)
+        expect -= abs(nu) * (q - up)
+    assert np.allclose(out, expect, rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("order,tw,tw2", [(2, 22, 2), (2, 20, 2), (2, 11, 1), (1, 10, 1),
+                                          (2, 0, 0)])
+def test_z_uniform_acoustics_is_the_2d_step(order, tw, tw2):
+    rng = np.random.default_rng(3 + tw)
+    mx, my, mz = 13, 11, 5
+    q2 = rng.normal(size=(3, mx, my))
+    q3 = np.zeros((4, mx, my, mz), order="F")
+    q3[:3] = q2[..., None]
+    dx, dy, dz, dt = 0.1, 0.12, 0.07, 0.01
+    bcl, bcu = [1, 3], [3, 1]
+    out3, cfl3 = ref.step3(AC3, PD3, q3, dx, dy, dz, dt, bcl + [2], bcu + [2], order, tw,
+                           [4, 4])
+    out2, cfl2, rc = ref.step(1, PD3, np.asfortranarray(q2), dx, dy, dt, bcl, bcu, order, tw2,
+                              [4, 4])
+    for l in range(mz):
+        assert rel_l1(out3[:3, :, :, l], out2) <= 1e-14
+    assert np.abs(out3[3]).max() <= 1e-14
+    assert cfl3 == pytest.approx(PD3[2] * dt / dz, rel=1e-15)
+
+
+@pytest.mark.parametrize("tw", [22, 11, 20])
+def test_conservation_periodic(tw):
+    rng = np.random.default_rng(4)
+    q = random3(4, (10, 9, 8), rng)
+    out, _ = ref.step3(AC3, PD3, q, 0.1, 0.1, 0.1, 0.02, [2] * 3, [2] * 3, 2, tw, [4, 4])
+    for k in range(4):
+        assert abs(out[k].sum() - q[k].sum()) <= 1e-13 * np.abs(q[k]).sum()
+
+
+def test_constant_state_preserved():
+    q = np.empty((4, 7, 6, 5), order="F")
+    q[:] = np.array([0.3, -1.2, 0.5, 2.0])[:, None, None, None]
+    out, _ = ref.step3(AC3, PD3, q, 0.1, 0.1, 0.1, 0.02, [1, 2, 1], [1, 2, 1], 2, 22, [4, 4])
+    assert np.array_equal(out, q)
+
+
+def test_cyclic_axis_permutation():
+    rng = np.random.default_rng(5)
+    q = random3(4, (9, 8, 7), rng)
+    dx, dy, dz, dt = 0.1, 0.13, 0.08, 0.012
+    a, ca = ref.step3(AC3, PD3, q, dx, dy, dz, dt, [1, 3, 2], [1, 3, 2], 2, 22, [4, 4])
+    # new axes (x', y', z') = (y, z, x): velocities (u', v', w') = (v, w, u)
+    qp = np.asfortranarray(q.transpose(0, 2, 3, 1)[[0, 2, 3, 1]])
+    b, cb = ref.step3(AC3, PD3, qp, dy, dz, dx, dt, [3, 2, 1], [3, 2, 1], 2, 22, [4, 4])
+    back = b[[0, 3, 1, 2]].transpose(0, 3, 1, 2)
+    assert rel_l1(back, a) <= 1e-14
+    assert ca == cb
+
+
+def test_unsupported_transverse_option():
+    q = random3(4, (4, 4, 4), np.random.default_rng(0))
+    with pytest.raises(ValueError):
+        ref.step3(AC3, PD3, q, 0.1, 0.1, 0.1, 0.01, [1] * 3, [1] * 3, 2, 21, [4, 4])
