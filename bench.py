@@ -65,6 +65,8 @@ def parse_args():
     p.add_argument("--batched-steps", type=int, default=200)
     p.add_argument("--no-adjoint", action="store_true")
     p.add_argument("--no-euler", action="store_true")
+    p.add_argument("--no-3d", action="store_true")
+    p.add_argument("--n3d", type=int, default=192, help="cube side of the 3D acoustics run")
     p.add_argument("--euler-steps", type=int, default=500)
     return p.parse_args()
 
@@ -350,6 +352,51 @@ def bench_euler(args, torch, world, device):
             "launches": 2 * (n + 3)}
 
 
+def bench_3d(args, torch, world, device):
+    """Unsplit 3D step (classic3, acoustics_3D, transverse_waves 22, MC):
+    a pressure pulse between walls on an n^3 cube, FP64, 40 device-controlled
+    steps (1.7 GB of state and workspace per 192^3, above L2), and the CPU
+    oracle on a 48^3 cube for reference."""
+    from clawpack_gb300 import workloads
+    from clawpack_gb300.device import DeviceProblem3
+
+    n, steps = args.n3d, 40
+    res = {}
+    for prob, k in ((workloads.acoustics_3d_pulse(32), 3), (workloads.acoustics_3d_pulse(n), steps)):
+        dev = DeviceProblem3(prob.solver_struct(), device=device)
+        dev.upload(prob.q0)
+        dev.ctrl_init(0.0, prob.dt_initial, math.inf, cfl_max=prob.cfl_max,
+                      cfl_desired=prob.cfl_desired, max_accepted=k, max_steps=10 * k)
+        torch.cuda.synchronize()
+        barrier(world)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        dev.advance(k)
+        e1.record()
+        torch.cuda.synchronize()
+        secs = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world, device)
+        c = dev.read_ctrl()
+        res = {"value": round(world * n ** 3 * c.numsteps / secs * 1e-9, 4),
+               "ms_per_step": round(secs / steps * 1e3, 3), "accepted_steps": int(c.numsteps),
+               "status": int(c.status)}
+        del dev
+    out = {"workload": f"acoustics_3d_pulse {n}^3, wall BCs, MC, transverse_waves 22 "
+                       f"(corner transport), CFL 0.9, FP64, {steps} steps",
+           "unit": UNIT, "fp64": res, "launches": 9 * (steps + 3)}
+    if int(os.environ.get("RANK", "0")) == 0:
+        from oracle import ref
+        small = workloads.acoustics_3d_pulse(48)
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ref.step3(1, small.problem_data, small.q0, *small.delta, small.dt_initial,
+                  small.bc_lower, small.bc_upper, 2, 22, [4, 4], nthreads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(48 ** 3 / dt * 1e-9, 5), "unit": UNIT,
+                               "cores": threads, "kind": "port",
+                               "sample": "one 48^3 step of the same problem, CPU oracle"}
+    return out
+
+
 def bench_adjoint(torch, world, device):
     """Gradient of the gauge least-squares loss with respect to the initial
     surface: 1024^2 shallow water, 500 steps, checkpoints every 23 steps,
@@ -518,6 +565,9 @@ def run_ours(args):
     if not args.no_euler:
         out["euler"] = bench_euler(args, torch, world, device)
         out["gpu_launches"] += out["euler"]["launches"]
+    if not args.no_3d:
+        out["acoustics_3d"] = bench_3d(args, torch, world, device)
+        out["gpu_launches"] += out["acoustics_3d"]["launches"]
     if not args.no_adjoint:
         out["adjoint"] = bench_adjoint(torch, world, device)
         out["gpu_launches"] += out["adjoint"]["launches"]

@@ -50,9 +50,33 @@ template <typename T>
 struct Rp3Acoustics {
     static constexpr int M = 4, MW = 2;
     struct Params {
-        T cc, zz;
+        T cc, zz, hz;  // hz = 1 / (2 zz)
     };
-    static Params make(const double *pd) { return Params{(T)pd[2], (T)pd[3]}; }
+    static Params make(const double *pd) {
+        return Params{(T)pd[2], (T)pd[3], (T)(1.0 / (2.0 * pd[3]))};
+    }
+    // The characteristic amplitude (x + zz y) / (2 zz): GCLAW_STRICT divides
+    // as the reference writes it, otherwise one multiply by 1 / (2 zz).
+    __device__ __forceinline__ static T amp(const Params &P, T x) {
+#ifdef GCLAW_STRICT
+        return x / ((T)2 * P.zz);
+#else
+        return x * P.hz;
+#endif
+    }
+
+    // Components of a transverse chain's flux entries that can be nonzero in
+    // sweep D: part 0 (G, faces normal to T1) or 1 (H, normal to T2); o = 1
+    // is the face's own row (single transverse + corner terms), o = 0, 2 the
+    // neighbouring rows (corner terms only).  Pressure and the transverse
+    // velocities only: the normal velocity is never split transversally.
+    template <int D>
+    __host__ __device__ static constexpr bool chain_nz(int part, int o, int k) {
+        constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+        if (k == 0) return true;
+        if (o == 1) return k == 1 + T1 || k == 1 + T2;
+        return k == 1 + (part == 0 ? T2 : T1);
+    }
 
     template <int D>
     __device__ __forceinline__ static void rpn3(const Params &P, const T *ql, const T *qr, T *W,
@@ -61,8 +85,8 @@ struct Rp3Acoustics {
         const T cc = P.cc, zz = P.zz;
         const T d0 = qr[0] - ql[0];
         const T d1 = qr[mn] - ql[mn];
-        const T a1 = (-d0 + zz * d1) / ((T)2 * zz);
-        const T a2 = (d0 + zz * d1) / ((T)2 * zz);
+        const T a1 = amp(P, -d0 + zz * d1);
+        const T a2 = amp(P, d0 + zz * d1);
 #pragma unroll
         for (int k = 0; k < 8; k++) W[k] = (T)0;
         W[0] = -a1 * zz; W[mn] = a1;
@@ -81,8 +105,8 @@ struct Rp3Acoustics {
     __device__ __forceinline__ static void rpt3(const Params &P, const T *asdq, T *bm, T *bp) {
         constexpr int mt = 1 + TA;
         const T cc = P.cc, zz = P.zz;
-        const T a1 = (-asdq[0] + zz * asdq[mt]) / ((T)2 * zz);
-        const T a2 = (asdq[0] + zz * asdq[mt]) / ((T)2 * zz);
+        const T a1 = amp(P, -asdq[0] + zz * asdq[mt]);
+        const T a2 = amp(P, asdq[0] + zz * asdq[mt]);
 #pragma unroll
         for (int k = 0; k < 4; k++) bm[k] = bp[k] = (T)0;
         bm[0] = cc * a1 * zz; bm[mt] = -cc * a1;
@@ -97,16 +121,41 @@ struct Rp3Acoustics {
     }
 };
 
-// Field planes of the workspace (doubles), per edge position.
+// Slot of chain entry (part, face s, row o, component k) among the entries
+// that can be nonzero in sweep D, or -1; and the number of slots.
+template <class RP, int D>
+__host__ __device__ constexpr int chain_slot(int part, int s, int o, int k) {
+    int n = 0;
+    for (int pp = 0; pp < 2; pp++)
+        for (int ss = 0; ss < 2; ss++)
+            for (int oo = 0; oo < 3; oo++)
+                for (int kk = 0; kk < RP::M; kk++) {
+                    if (!RP::template chain_nz<D>(pp, oo, kk)) continue;
+                    if (pp == part && ss == s && oo == o && kk == k) return n;
+                    n++;
+                }
+    return -1;
+}
+template <class RP, int D>
+__host__ __device__ constexpr int chain_slots() {
+    int n = 0;
+    for (int pp = 0; pp < 2; pp++)
+        for (int ss = 0; ss < 2; ss++)
+            for (int oo = 0; oo < 3; oo++)
+                for (int kk = 0; kk < RP::M; kk++) n += RP::template chain_nz<D>(pp, oo, kk);
+    return n;
+}
+
+// Field planes of the workspace (doubles), per edge position: the edge
+// record of k_edges, then the correction flux and the A-dQ / A+dQ chains of
+// k_chains (the slots that can be nonzero; the count is the same in every
+// sweep).
 template <class RP>
 struct Fields {
-    static constexpr int M = RP::M, MW = RP::MW;
+    static constexpr int M = RP::M, MW = RP::MW, NCH = chain_slots<RP, 0>();
+    static_assert(NCH == chain_slots<RP, 1>() && NCH == chain_slots<RP, 2>(), "slot count");
     static constexpr int W = 0, S = MW * M, AM = S + MW, AP = AM + M, FA = AP + M;
-    static constexpr int AMC = FA + M, APC = AMC + 12 * M, NF = APC + 12 * M;
-    // chain entry (G: part 0, H: part 1; face s 0/1; t-offset o 0..2)
-    __host__ __device__ static constexpr int ce(int part, int s, int o, int k) {
-        return part * 6 * M + (s * 3 + o) * M + k;
-    }
+    static constexpr int AMC = FA + M, APC = AMC + NCH, NF = APC + NCH;
 };
 
 // Box position of (x, y, z), each in [-1, n + 1].
@@ -290,8 +339,10 @@ __device__ __forceinline__ void chain(const typename RP::Params &P, const double
         for (int o = 0; o < 3; o++)
 #pragma unroll
             for (int k = 0; k < M; k++) {
-                ws[(long long)(base + F::ce(0, s, o, k)) * np + idx] = g[s][o][k];
-                ws[(long long)(base + F::ce(1, s, o, k)) * np + idx] = hh[s][o][k];
+                if (RP::template chain_nz<D>(0, o, k))
+                    ws[(long long)(base + chain_slot<RP, D>(0, s, o, k)) * np + idx] = g[s][o][k];
+                if (RP::template chain_nz<D>(1, o, k))
+                    ws[(long long)(base + chain_slot<RP, D>(1, s, o, k)) * np + idx] = hh[s][o][k];
             }
 }
 
@@ -389,7 +440,7 @@ __global__ void __launch_bounds__(NT3) k_chains(const Args3 a,
         chain<RP, D>(P, ap, dbl, h, f1, f2, ws, np, idx, F::APC);
     } else {
 #pragma unroll
-        for (int e = 0; e < 12 * M; e++) {
+        for (int e = 0; e < F::NCH; e++) {
             ws[(long long)(F::AMC + e) * np + idx] = 0.0;
             ws[(long long)(F::APC + e) * np + idx] = 0.0;
         }
@@ -423,7 +474,9 @@ __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
 #pragma unroll
         for (int k = 0; k < M; k++) v[k] = src[o + k];
         const int c = p[D], A = p[T1], B = p[T2];
+#pragma unroll
         for (int db = -1; db <= 1; db++)
+#pragma unroll
             for (int da = -1; da <= 1; da++) {
                 int e0[3];
                 e0[D] = c; e0[T1] = A - da; e0[T2] = B - db;
@@ -432,9 +485,12 @@ __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
                 const long long i0 = bpos(a, e0[0], e0[1], e0[2]);
                 const long long i1 = bpos(a, e1[0], e1[1], e1[2]);
                 // flux entry (part, face s, offset o) of this slice at cell c
+                // (entries that cannot be nonzero are +0, as stored by the oracle)
                 auto ent = [&](int part, int s, int off, int k) {
-                    const double am = ws[(long long)(F::AMC + F::ce(part, s, off + 1, k)) * np + i1];
-                    const double ap = ws[(long long)(F::APC + F::ce(part, s, off + 1, k)) * np + i0];
+                    const int slot = chain_slot<RP, D>(part, s, off + 1, k);
+                    if (slot < 0) return (0.0 + 0.0) + 0.0;
+                    const double am = ws[(long long)(F::AMC + slot) * np + i1];
+                    const double ap = ws[(long long)(F::APC + slot) * np + i0];
                     return (0.0 + am) + ap;
                 };
 #pragma unroll

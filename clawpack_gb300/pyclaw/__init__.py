@@ -8,5 +8,5 @@ ClawSolver2D, BC and limiters.tvd.
 from . import limiters  # noqa: F401
 from .controller import Controller  # noqa: F401
 from .geometry import Dimension, Domain, Grid, Patch  # noqa: F401
-from .solver import BC, ClawSolver2D  # noqa: F401
+from .solver import BC, ClawSolver2D, ClawSolver3D  # noqa: F401
 from .state import Solution, State  # noqa: F401

@@ -24,7 +24,7 @@ import math
 import numpy as np
 
 from .. import _lib
-from ..device import DeviceProblem, make_solver_struct
+from ..device import DeviceProblem, DeviceProblem3, make_solver3_struct, make_solver_struct
 from .limiters import tvd
 
 
@@ -128,6 +128,8 @@ class ClawSolver2D:
     def _check_options(self, state):
         if self.rp is None:
             raise ValueError("solver.rp is not set")
+        if getattr(self.rp, "num_dim", 2) != 2:
+            raise ValueError(f"{self.rp.name} is not a 2D Riemann solver")
         if self.kernel_language != "CUDA":
             raise NotImplementedError(
                 f"kernel_language={self.kernel_language!r}: this framework provides the 'CUDA' "
@@ -367,3 +369,84 @@ class ClawSolver2D:
                 else:
                     dt = self.dt_max
         return t, dt, parity, numsteps, cflmax, cfl, dtmin, dtmax, _lib.MAX_STEPS
+
+
+class ClawSolver3D(ClawSolver2D):
+    """PyClaw's ClawSolver3D (upstream pyclaw/src/pyclaw/classic/solver.py)
+    on the CUDA backend: the unsplit 3D step of gclaw3.h.
+
+    ``transverse_waves`` takes ClawSolver3D's values: 0, 10 / 11
+    (``trans_inc``: transverse propagation of the increment waves, without /
+    with the corner terms) and 20 / 22 (``trans_cor``: also of the correction
+    waves).  Steps are unsplit (``dimensional_split = False``), FP64, without
+    aux arrays."""
+    no_trans = 0
+    trans_inc = 11
+    trans_cor = 22
+
+    def __init__(self, riemann_solver=None, claw_package=None):
+        super().__init__(riemann_solver, claw_package)
+        self.num_dim = 3
+        self.transverse_waves = self.trans_cor
+        self.bc_lower = [None, None, None]
+        self.bc_upper = [None, None, None]
+        self.aux_bc_lower = [None, None, None]
+        self.aux_bc_upper = [None, None, None]
+        self.reflect_index = [1, 2, 3]
+
+    def _problem_data(self, state):
+        pd = state.problem_data
+        rho = float(pd["rho"])
+        bulk = float(pd["bulk"])
+        cc = float(pd["cc"]) if "cc" in pd else math.sqrt(bulk / rho)
+        zz = float(pd["zz"]) if "zz" in pd else rho * cc
+        return [rho, bulk, cc, zz]
+
+    def _check_options(self, state):
+        if self.rp is None:
+            raise ValueError("solver.rp is not set")
+        if getattr(self.rp, "num_dim", 2) != 3:
+            raise ValueError(f"{self.rp.name} is not a 3D Riemann solver")
+        if self.kernel_language != "CUDA":
+            raise NotImplementedError(
+                f"kernel_language={self.kernel_language!r}: this framework provides the 'CUDA' "
+                "backend only")
+        if self.fwave:
+            raise ValueError(f"{self.rp.name} needs solver.fwave = False")
+        if self.dimensional_split:
+            raise NotImplementedError("3D steps are unsplit here; set "
+                                      "solver.dimensional_split = False")
+        if state.num_aux or getattr(state, "index_capa", -1) >= 0:
+            raise NotImplementedError("3D steps with aux arrays are not supported")
+        if self.num_ghost != 2:
+            raise ValueError("num_ghost must be 2")
+        if self.transverse_waves not in (0, 10, 11, 20, 22):
+            raise NotImplementedError("transverse_waves must be 0, 10, 11, 20 or 22")
+        for b in list(self.bc_lower) + list(self.bc_upper):
+            if b is None:
+                raise ValueError("boundary conditions are not set")
+            if b == BC.custom:
+                raise NotImplementedError("BC.custom is not supported by the CUDA backend")
+        if self.precision != "fp64":
+            raise NotImplementedError("3D steps are FP64 (solver.precision = 'fp64')")
+        if self.step_source is not None and self.source_split not in (1, 2):
+            raise ValueError("solver.source_split must be 1 (Godunov) or 2 (Strang)")
+
+    def solver_struct(self, state):
+        """The gclaw3_solver C struct for this solver and grid."""
+        self._check_options(state)
+        g = state.grid
+        mx, my, mz = g.num_cells
+        dx, dy, dz = g.delta
+        return make_solver3_struct(self.rp.rp_id, mx, my, mz, dx, dy, dz, self.bc_lower,
+                                   self.bc_upper, self._mthlim, self.order,
+                                   self.transverse_waves, _lib.PREC_FP64,
+                                   self._problem_data(state))
+
+    def _device(self, state):
+        s = self.solver_struct(state)
+        key = (bytes(s), False)
+        if self._dev is None or self._dev_key != key:
+            self._dev = DeviceProblem3(s)
+            self._dev_key = key
+        return self._dev

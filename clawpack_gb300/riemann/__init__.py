@@ -15,12 +15,13 @@ from .. import _lib
 from . import static
 
 
-def _descriptor(name, rp_id, fwave=False):
+def _descriptor(name, rp_id, fwave=False, num_dim=2):
     # cparam plays the role of the f2py module's Fortran common block, which
     # PyClaw fills from state.problem_data before stepping.
     return SimpleNamespace(__name__=f"clawpack_gb300.riemann.{name}", name=name, rp_id=rp_id,
                            num_eqn=static.num_eqn[name], num_waves=static.num_waves[name],
-                           num_aux=static.num_aux[name], fwave=fwave, cparam=SimpleNamespace())
+                           num_aux=static.num_aux[name], fwave=fwave, num_dim=num_dim,
+                           cparam=SimpleNamespace())
 
 
 acoustics_2D = _descriptor("acoustics_2D", _lib.RP_ACOUSTICS_2D)
@@ -34,5 +35,8 @@ vc_acoustics_2D = _descriptor("vc_acoustics_2D", _lib.RP_VC_ACOUSTICS_2D)
 shallow_bathymetry_fwave_2D = _descriptor("shallow_bathymetry_fwave_2D",
                                           _lib.RP_SHALLOW_BATHYMETRY_FWAVE_2D, fwave=True)
 
+# 3D (ClawSolver3D): constant-coefficient acoustics, q = (p, u, v, w)
+acoustics_3D = _descriptor("acoustics_3D", _lib.RP3_ACOUSTICS_3D, num_dim=3)
+
 __all__ = ["acoustics_2D", "shallow_roe_with_efix_2D", "euler_4wave_2D", "vc_acoustics_2D",
-           "shallow_bathymetry_fwave_2D", "static"]
+           "shallow_bathymetry_fwave_2D", "acoustics_3D", "static"]

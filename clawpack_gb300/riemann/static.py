@@ -5,6 +5,7 @@ num_eqn = {
     "euler_4wave_2D": 4,
     "vc_acoustics_2D": 3,
     "shallow_bathymetry_fwave_2D": 3,
+    "acoustics_3D": 4,
 }
 num_aux = {
     "acoustics_2D": 0,
@@ -12,6 +13,7 @@ num_aux = {
     "euler_4wave_2D": 0,
     "vc_acoustics_2D": 2,
     "shallow_bathymetry_fwave_2D": 1,
+    "acoustics_3D": 0,
 }
 num_waves = {
     "acoustics_2D": 2,
@@ -19,4 +21,5 @@ num_waves = {
     "euler_4wave_2D": 4,
     "vc_acoustics_2D": 2,
     "shallow_bathymetry_fwave_2D": 3,
+    "acoustics_3D": 2,
 }

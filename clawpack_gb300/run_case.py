@@ -34,7 +34,8 @@ def make_workload(name, mx, my):
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("--workload", default="shallow", choices=["shallow", "euler", "acoustics"])
+    p.add_argument("--workload", default="shallow",
+                   choices=["shallow", "euler", "acoustics", "acoustics3d"])
     p.add_argument("--mx", type=int, default=2048)
     p.add_argument("--my", type=int, default=None)
     p.add_argument("--steps", type=int, default=20)
@@ -53,6 +54,8 @@ def main(argv=None):
     _lib.lib().gclaw_fp64_kernel({"auto": 0, "tile": 1, "strip": 2}[a.fp64_kernel])
     if a.batched:
         return run_batched(a)
+    if a.workload == "acoustics3d":
+        return run_3d(a)
     w = make_workload(a.workload, a.mx, a.my or a.mx)
     s = w.solver_struct(0 if a.precision == "fp64" else 1)
     dev = DeviceProblem(s, split=a.split)
@@ -72,6 +75,31 @@ def main(argv=None):
     cells = w.mx * w.my
     print(json.dumps({"workload": w.name, "mx": w.mx, "my": w.my, "precision": a.precision,
                       "split": a.split, "steps": a.steps, "ms_per_step": ms,
+                      "gcell_updates_per_s": cells / (ms * 1e-3) * 1e-9 if ms > 0 else None,
+                      "accepted": c.numsteps, "status": c.status, "cfl": c.cfl}))
+    return 0 if c.status == 0 else 1
+
+
+def run_3d(a):
+    """--warmup then --steps device-controlled 3D steps on an mx^3 cube."""
+    from .device import DeviceProblem3
+
+    w = workloads.acoustics_3d_pulse(a.mx)
+    dev = DeviceProblem3(w.solver_struct())
+    dev.upload(w.q0)
+    dev.ctrl_init(0.0, w.dt_initial, math.inf, cfl_max=w.cfl_max, cfl_desired=w.cfl_desired,
+                  max_steps=10 ** 9)
+    dev.advance(a.warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    dev.advance(a.steps)
+    e1.record()
+    c = dev.read_ctrl()
+    ms = e0.elapsed_time(e1) / max(a.steps, 1)
+    cells = w.n ** 3
+    print(json.dumps({"workload": w.name, "n": w.n, "precision": "fp64", "steps": a.steps,
+                      "ms_per_step": ms,
                       "gcell_updates_per_s": cells / (ms * 1e-3) * 1e-9 if ms > 0 else None,
                       "accepted": c.numsteps, "status": c.status, "cfl": c.cfl}))
     return 0 if c.status == 0 else 1

@@ -321,3 +321,38 @@ def adjoint_problem(mx=1024, my=None, nsteps=500, checkpoint_every=23, seed=ADJO
     h_true = _bumps(rng, mx, my)
     gauges = np.stack([rng.integers(0, mx, 64), rng.integers(0, my, 64)], axis=1)
     return AdjointProblem(mx, my, nsteps, checkpoint_every, h0, h_true, gauges, limiter=limiter)
+
+
+@dataclass
+class Workload3:
+    """A 3D problem: acoustics_3D on a cube, state (4, n, n, n)."""
+    name: str
+    n: int
+    delta: tuple
+    q0: np.ndarray
+    problem_data: list
+    bc_lower: list
+    bc_upper: list
+    dt_initial: float
+    cfl_desired: float = 0.9
+    cfl_max: float = 1.0
+
+    def solver_struct(self, order=2, tw=22, lim=tvd.MC):
+        from .device import make_solver3_struct
+
+        return make_solver3_struct(_lib.RP3_ACOUSTICS_3D, self.n, self.n, self.n, *self.delta,
+                                   self.bc_lower, self.bc_upper, [lim, lim], order, tw,
+                                   _lib.PREC_FP64, self.problem_data)
+
+
+def acoustics_3d_pulse(n=192):
+    """A Gaussian pressure pulse off the centre of [-1, 1]^3 between walls;
+    rho = 1, bulk = 4 (c = 2), MC limiter, transverse_waves 22."""
+    x = _centers(-1.0, 1.0, n)
+    X, Y, Z = np.meshgrid(x, x, x, indexing="ij")
+    q = np.zeros((4, n, n, n), order="F")
+    q[0] = np.exp(-40.0 * ((X - 0.2) ** 2 + (Y + 0.1) ** 2 + Z ** 2))
+    h = 2.0 / n
+    # first dt from the sound speed, so no attempt is rejected
+    return Workload3("acoustics_3d_pulse", n, (h, h, h), q, [1.0, 4.0, 2.0, 2.0],
+                     [BC.wall] * 3, [BC.wall] * 3, dt_initial=0.9 * h / 2.0)

@@ -107,3 +107,36 @@ def test_refusals(cuda):
     assert L.gclaw3_check(ctypes.byref(s)) == 0
     s.mz = 1
     assert L.gclaw3_check(ctypes.byref(s)) == _lib.ERR_ARG
+
+
+def test_controller_run_through_clawsolver3d(cuda, oracle):
+    from clawpack_gb300 import pyclaw, riemann
+
+    dims = [pyclaw.Dimension(-1.0, 1.0, n, name=c) for n, c in ((20, "x"), (18, "y"), (16, "z"))]
+    domain = pyclaw.Domain(dims)
+    state = pyclaw.State(domain, 4)
+    state.problem_data.update(rho=1.0, bulk=4.0)
+    X, Y, Z = state.grid.p_centers
+    state.q[0] = np.exp(-20.0 * ((X - 0.2) ** 2 + Y ** 2 + (Z + 0.1) ** 2))
+    solver = pyclaw.ClawSolver3D(riemann.acoustics_3D)
+    solver.dimensional_split = False
+    solver.limiters = pyclaw.limiters.tvd.MC
+    solver.bc_lower = [pyclaw.BC.extrap, pyclaw.BC.wall, pyclaw.BC.periodic]
+    solver.bc_upper = [pyclaw.BC.extrap, pyclaw.BC.wall, pyclaw.BC.periodic]
+    solver.dt_initial = 0.01
+    claw = pyclaw.Controller()
+    claw.solution = pyclaw.Solution(state, domain)
+    claw.solver = solver
+    claw.tfinal, claw.num_output_times = 0.3, 3
+    q0 = state.q.copy()
+    claw.run()
+    d = tuple(state.grid.delta)
+    bcl, bcu = [1, 3, 2], [1, 3, 2]
+
+    def step(qq, dt):
+        return oracle.step3(1, PD3, qq, *d, dt, bcl, bcu, 2, 22, [4, 4], nthreads=8)
+
+    q, t, dt = q0, 0.0, 0.01
+    for k in range(1, 4):
+        q, t, dt, _ = oracle.evolve(step, q, t, 0.1 * k, dt, cfl_desired=0.9, cfl_max=1.0)
+        assert rel_l1(claw.frames[k].q, q) <= 1e-12, k

@@ -116,3 +116,23 @@ def test_fwave_solver_front_end():
     claw = workloads.make_claw(workloads.shallow_dam_break(8, 8))
     with pytest.raises(ValueError):  # and the other solvers fwave = False
         s2.solver_struct(claw.solution.state)
+
+
+def test_clawsolver3d_front_end():
+    dims = [pyclaw.Dimension(0.0, 1.0, n, name=c) for n, c in ((8, "x"), (6, "y"), (5, "z"))]
+    st = pyclaw.State(pyclaw.Domain(dims), 4)
+    st.problem_data.update(rho=1.0, bulk=4.0)
+    s = pyclaw.ClawSolver3D(riemann.acoustics_3D)
+    assert s.transverse_waves == s.trans_cor == 22 and s.trans_inc == 11
+    s.bc_lower = s.bc_upper = [pyclaw.BC.wall] * 3
+    with pytest.raises(NotImplementedError):  # 3D steps are unsplit here
+        s.solver_struct(st)
+    s.dimensional_split = False
+    ss = s.solver_struct(st)
+    assert (ss.mx, ss.my, ss.mz) == (8, 6, 5) and list(ss.problem_data)[:4] == [1, 4, 2, 2]
+    s.transverse_waves = 21
+    with pytest.raises(NotImplementedError):
+        s.solver_struct(st)
+    s2 = pyclaw.ClawSolver2D(riemann.acoustics_3D)
+    with pytest.raises(ValueError):  # a 3D solver in the 2D class
+        s2.solver_struct(st)
