@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(STRIP_NW * 32, StripCfg<RPT>::MINB)
 }
 
 template <template <typename> class RPT, typename T, int TX, int TY, int NT>
-__global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1)
+__global__ void __launch_bounds__(NT, tile_min_blocks<T, NT>())
     batch_step_kernel(const StepArgs base, const typename RPT<T>::Params P,
                       const BatchEntry *__restrict__ ent, const int *__restrict__ tstart,
                       int nprob, int total_tiles, double *q0, double *q1, gclaw_ctrl *ctrls) {

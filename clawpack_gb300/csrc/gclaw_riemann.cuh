@@ -127,6 +127,52 @@ __device__ __forceinline__ double max_abs<double>(double m, double s) {
     return a <= F64_INF_BITS && a > b ? __longlong_as_double(a) : m;
 }
 
+// Reciprocal for the product build.  T = float: the division (approximate
+// under -prec-div=false).  T = double: Newton-Raphson iteration for 1/a
+// (r <- r + r (1 - a r), quadratic convergence; J.-M. Muller et al.,
+// Handbook of Floating-Point Arithmetic, 2nd ed., sec. 4.7) from a seed
+// built on the integer and FP32 pipes: the mantissa of a, truncated to a
+// float in [1, 2), its FP32 reciprocal, and the exponent of a subtracted
+// with an integer add.  The seed is within 2^-22 of 1/a, so two iterations
+// (four FP64 fused multiply-adds) reach the last bit or two of the double;
+// GB300 executes FP64 arithmetic at 1/64 of its FP32 rate, and the IEEE
+// division costs several more FP64 instructions.  Non-positive, denormal,
+// infinite, NaN and very large a (exponent field 0, >= 2045) take the
+// IEEE division.
+template <typename T>
+__device__ __forceinline__ T rcp_fast(T a) { return (T)1 / a; }
+static __device__ __noinline__ double rcp_slow(double a) { return 1.0 / a; }
+template <>
+__device__ __forceinline__ double rcp_fast<double>(double a) {
+    const long long b = __double_as_longlong(a);
+    const int e = (int)((b >> 52) & 0x7ff);  // biased exponent
+    if (b <= 0 || e == 0 || e >= 2045) return rcp_slow(a);
+    const float mf = __int_as_float(0x3f800000 | (int)((b >> 29) & 0x7fffff));  // in [1, 2)
+    const float rf = __frcp_rn(mf);                                             // in (0.5, 1]
+    const unsigned u = __float_as_uint(rf);
+    // rf as a double, with the exponent of a taken off: 2^(1023 - e) / m
+    const long long rb = ((long long)((u >> 23) + 896 + 1023 - e) << 52) |
+                         ((long long)(u & 0x7fffff) << 29);
+    double r = __longlong_as_double(rb);
+    double t = fma(-a, r, 1.0);
+    r = fma(r, t, r);
+    t = fma(-a, r, 1.0);
+    return fma(r, t, r);
+}
+
+// a / b: the division in GCLAW_STRICT and FP32, a times the Newton-Raphson
+// reciprocal of b for FP64 in the product build (repeated divisors share
+// one reciprocal after inlining).
+template <typename T>
+__device__ __forceinline__ T qdiv(T a, T b) {
+#ifdef GCLAW_STRICT
+    return a / b;
+#else
+    if constexpr (sizeof(T) == 8) return a * rcp_fast(b);
+    else return a / b;
+#endif
+}
+
 // copysign(1, s) * x, exactly, as a sign-bit exchange on the integer pipes.
 template <typename T>
 __device__ __forceinline__ T sign_times(T x, T s);
@@ -327,7 +373,7 @@ struct RpShallow {
         aux[4] = q[2] / q[0];
         aux[5] = sqrt(P.g * q[0]);
 #else
-        const T rh = (T)1 / q[0];
+        const T rh = rcp_fast(q[0]);
         aux[3] = q[1] * rh;
         aux[4] = q[2] * rh;
         aux[1] = aux[3] * hs;
@@ -359,7 +405,7 @@ struct RpShallow {
             c = sqrt(P.g * hbar);
 #else
             // one reciprocal for both averages; c and 0.5 / c from one rsqrt
-            const T ri = (T)1 / hsq2;
+            const T ri = rcp_fast(hsq2);
             u = (al[mu] + ar[mu]) * ri;
             v = (al[mv] + ar[mv]) * ri;
             const T gh = P.g * hbar;
@@ -547,7 +593,7 @@ struct RpShallowFwave {
         const T b1 = (s[2] * d0 - d1) / (s[2] - s[0]);
         const T b3 = (d1 - s[0] * d0) / (s[2] - s[0]);
 #else
-        const T rd = (T)1 / (s[2] - s[0]);
+        const T rd = rcp_fast(s[2] - s[0]);
         const T b1 = (s[2] * d0 - d1) * rd;
         const T b3 = (d1 - s[0] * d0) * rd;
 #endif
@@ -608,7 +654,7 @@ struct RpEuler {
     }
 
     __device__ __forceinline__ static T pressure(T gamma1, const T *q) {
-        return gamma1 * (q[3] - (T)0.5 * (q[1] * q[1] + q[2] * q[2]) / q[0]);
+        return gamma1 * (q[3] - qdiv((T)0.5 * (q[1] * q[1] + q[2] * q[2]), q[0]));
     }
 
     // aux = (sqrt rho, p, rho u / sqrt rho, rho v / sqrt rho, (E + p) / sqrt rho,
@@ -618,12 +664,12 @@ struct RpEuler {
         const T p = pressure(P.gamma1, q);
         aux[0] = rs;
         aux[1] = p;
-        aux[2] = q[1] / rs;
-        aux[3] = q[2] / rs;
-        aux[4] = (q[3] + p) / rs;
-        aux[5] = q[1] / q[0];
-        aux[6] = q[2] / q[0];
-        aux[7] = sqrt(P.gamma * p / q[0]);
+        aux[2] = qdiv(q[1], rs);
+        aux[3] = qdiv(q[2], rs);
+        aux[4] = qdiv(q[3] + p, rs);
+        aux[5] = qdiv(q[1], q[0]);
+        aux[6] = qdiv(q[2], q[0]);
+        aux[7] = sqrt(qdiv(P.gamma * p, q[0]));
     }
 
     template <int IXY>
@@ -643,21 +689,21 @@ struct RpEuler {
             enth = (T)((((double)ql[3] + (double)pl) / rl + ((double)qr[3] + (double)pr) / rr) / rs);
         } else {
             const T rhsq2 = al[0] + ar[0];
-            u = (al[1 + mu] + ar[1 + mu]) / rhsq2;
-            v = (al[1 + mv] + ar[1 + mv]) / rhsq2;
-            enth = (al[4] + ar[4]) / rhsq2;
+            u = qdiv(al[1 + mu] + ar[1 + mu], rhsq2);
+            v = qdiv(al[1 + mv] + ar[1 + mv], rhsq2);
+            enth = qdiv(al[4] + ar[4], rhsq2);
         }
         T u2v2 = u * u + v * v;
         T c2 = gamma1 * (enth - (T)0.5 * u2v2);
         bool bad = !(c2 > (T)0);
         T a = sqrt(c2);
-        T g1a2 = gamma1 / c2;
+        T g1a2 = qdiv(gamma1, c2);
         T euv = enth - u2v2;
         R[0] = u; R[1] = v; R[2] = enth; R[3] = u2v2; R[4] = a; R[5] = g1a2; R[6] = euv;
         T d0 = qr[0] - ql[0], dmu = qr[mu] - ql[mu], dmv = qr[mv] - ql[mv], d3 = qr[3] - ql[3];
         T a3 = g1a2 * (euv * d0 + u * dmu + v * dmv - d3);
         T a2 = dmv - v * d0;
-        T a4 = (dmu + (a - u) * d0 - a * a3) / ((T)2 * a);
+        T a4 = qdiv(dmu + (a - u) * d0 - a * a3, (T)2 * a);
         T a1 = d0 - a3 - a4;
         T *w1 = W, *w2 = W + 4, *w3 = W + 8, *w4 = W + 12;
         w1[0] = a1; w1[mu] = a1 * (u - a); w1[mv] = a1 * v; w1[3] = a1 * (enth - u * a);
@@ -696,9 +742,9 @@ struct RpEuler {
             T rhou1 = ql[mu] + w1[mu];
             T rhov1 = ql[mv] + w1[mv];
             T en1 = ql[3] + w1[3];
-            T p1 = gamma1 * (en1 - (T)0.5 * (rhou1 * rhou1 + rhov1 * rhov1) / rho1);
-            T c1 = sqrt(gamma * p1 / rho1);
-            T s1 = rhou1 / rho1 - c1;
+            T p1 = gamma1 * (en1 - qdiv((T)0.5 * (rhou1 * rhou1 + rhov1 * rhov1), rho1));
+            T c1 = sqrt(qdiv(gamma * p1, rho1));
+            T s1 = qdiv(rhou1, rho1) - c1;
             T sfract;
             if (s0 < (T)0 && s1 > (T)0)
                 sfract = s0 * (s1 - s[0]) / (s1 - s0);
@@ -718,9 +764,9 @@ struct RpEuler {
                 T rhou2 = qr[mu] - w4[mu];
                 T rhov2 = qr[mv] - w4[mv];
                 T en2 = qr[3] - w4[3];
-                T p2 = gamma1 * (en2 - (T)0.5 * (rhou2 * rhou2 + rhov2 * rhov2) / rho2);
-                T cc2 = sqrt(gamma * p2 / rho2);
-                T s2 = rhou2 / rho2 + cc2;
+                T p2 = gamma1 * (en2 - qdiv((T)0.5 * (rhou2 * rhou2 + rhov2 * rhov2), rho2));
+                T cc2 = sqrt(qdiv(gamma * p2, rho2));
+                T s2 = qdiv(rhou2, rho2) + cc2;
                 bool add = true;
                 if (s2 < (T)0 && s3 > (T)0)
                     sfract = s2 * (s3 - s[3]) / (s3 - s2);
@@ -751,7 +797,7 @@ struct RpEuler {
         T u = R[0], v = R[1], enth = R[2], u2v2 = R[3], a = R[4], g1a2 = R[5], euv = R[6];
         T a3 = g1a2 * (euv * asdq[0] + u * asdq[mu] + v * asdq[mv] - asdq[3]);
         T a2 = asdq[mu] - u * asdq[0];
-        T a4 = (asdq[mv] + (a - v) * asdq[0] - a * a3) / ((T)2 * a);
+        T a4 = qdiv(asdq[mv] + (a - v) * asdq[0] - a * a3, (T)2 * a);
         T a1 = asdq[0] - a3 - a4;
         T wb[16], sb[4];
         wb[0] = a1; wb[mu] = a1 * u; wb[mv] = a1 * (v - a); wb[3] = a1 * (enth - v * a);

@@ -36,7 +36,7 @@
 namespace gclaw {
 
 template <template <typename> class RPT, typename T, int TX, int TY, int NT>
-__global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1) step_kernel(const StepArgs a,
+__global__ void __launch_bounds__(NT, tile_min_blocks<T, NT>()) step_kernel(const StepArgs a,
                                                   const typename RPT<T>::Params P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double s_dt, s_dtdx, s_dtdy;
@@ -710,7 +710,7 @@ struct NoallocHeader {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
 template <template <typename> class RPT, typename T, int TX, int TY, int NT>
-__global__ void __launch_bounds__(NT, NT <= 512 ? 2 : 1)
+__global__ void __launch_bounds__(NT, tile_min_blocks<T, NT>())
     step_kernel_noalloc(const StepArgs a, const typename RPT<T>::Params P,
                         unsigned char *__restrict__ scratch) {
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -260,6 +260,15 @@ struct CapaTileCfg {
         capa_fit_ty<typename Capa<RPT>::template rp<T>, T, TX, TileCfg<RPT, T>::TY>();
 };
 
+// Resident CTAs per SM the tile kernels are compiled for (the register cap):
+// two, except FP64 tiles of more than 256 threads, which hold one CTA per SM
+// anyway (their per-tile aux area fills the shared memory) and may then use
+// up to 128 registers a thread.
+template <typename T, int NT>
+__host__ __device__ constexpr int tile_min_blocks() {
+    return (NT <= 256 || sizeof(T) == 4) && NT <= 512 ? 2 : 1;
+}
+
 // Cells per CTA of the kernel that runs solver rp at the given precision.
 static inline void tile_shape(int rp, int precision, int *tx, int *ty) {
     const bool f64 = precision == GCLAW_PREC_FP64;
@@ -518,7 +527,11 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
                 // (1-4), so the quotient is only taken for dot > 0
                 T phi = (T)0;
                 if (!le0(dot)) {
+#ifdef GCLAW_STRICT
                     const T th = dot / wn2;
+#else
+                    const T th = dot * rcp_fast(wn2);
+#endif
                     phi = gt0(th) ? philim_pos<T>(lim, th) : philim<T>(lim, th);
                 }
 #pragma unroll

@@ -133,7 +133,11 @@ __device__ __forceinline__ void strip_limit_edge(const typename RP::Params &P, T
             }
             T phi = (T)0;
             if (!le0(dot)) {
+#ifdef GCLAW_STRICT
                 const T th = dot / wn2;
+#else
+                const T th = dot * rcp_fast(wn2);
+#endif
                 phi = gt0(th) ? philim_pos<T>(lim, th) : philim<T>(lim, th);
             }
 #pragma unroll
