@@ -288,6 +288,12 @@ static int launch_capa(const gclaw_solver *s, const StepArgs &a, cudaStream_t st
     return launch_tile<Capa<RPT>::template rp, double, C::TX, C::TY, C::NT>(s, a, st, nlaunch);
 }
 
+// The product build's FP64 reciprocal over an array (gclaw_rcp_fp64).
+__global__ void rcp_kernel(const double *__restrict__ x, double *__restrict__ y, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = qdiv(1.0, x[i]);
+}
+
 static int dispatch(const gclaw_solver *s, const StepArgs &a, cudaStream_t st, int nlaunch) {
     const bool f64 = s->precision == GCLAW_PREC_FP64;
     if (s->capa) {
@@ -481,6 +487,14 @@ int gclaw_fp32_kernel(int which) {
     const int prev = g_fp32_kernel;
     if (which >= 0 && which <= 2) g_fp32_kernel = which;
     return prev;
+}
+
+int gclaw_rcp_fp64(const double *x_dev, double *y_dev, long long n, void *stream) {
+    if (!x_dev || !y_dev || n < 0) return GCLAW_ERR_ARG;
+    if (n == 0) return GCLAW_OK;
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    rcp_kernel<<<nb, 256, 0, (cudaStream_t)stream>>>(x_dev, y_dev, n);
+    return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
 }
 
 int gclaw_fp64_kernel(int which) {

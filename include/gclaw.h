@@ -162,6 +162,13 @@ int gclaw_fp32_kernel(int which);
  * strips (bit-identical to tiles with -fmad=false). */
 int gclaw_fp64_kernel(int which);
 
+/* y[i] = 1 / x[i] with the reciprocal the product build uses for FP64
+ * divisions (a Newton-Raphson iteration from an FP32 seed; IEEE division
+ * for non-positive, denormal, infinite, NaN and very large x), n device
+ * values, asynchronous on stream -- exposed so its error can be measured.
+ * libgclaw_strict.so, which divides exactly, exports it too. */
+int gclaw_rcp_fp64(const double *x_dev, double *y_dev, long long n, void *stream);
+
 /* Drop-in for classic2.step2 (upstream pyclaw/src/pyclaw/classic/step2.f90):
  * one unsplit step of a ghost-filled qbc.  qold_dev and qnew_dev are
  * (num_eqn, mx+4, my+4) Fortran order; the interior of qnew_dev receives the
