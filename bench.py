@@ -361,28 +361,33 @@ def bench_3d(args, torch, world, device):
     from clawpack_gb300.device import DeviceProblem3
 
     n, steps = args.n3d, 40
-    res = {}
-    for prob, k in ((workloads.acoustics_3d_pulse(32), 3), (workloads.acoustics_3d_pulse(n), steps)):
-        dev = DeviceProblem3(prob.solver_struct(), device=device)
-        dev.upload(prob.q0)
-        dev.ctrl_init(0.0, prob.dt_initial, math.inf, cfl_max=prob.cfl_max,
-                      cfl_desired=prob.cfl_desired, max_accepted=k, max_steps=10 * k)
-        torch.cuda.synchronize()
-        barrier(world)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        dev.advance(k)
-        e1.record()
-        torch.cuda.synchronize()
-        secs = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world, device)
-        c = dev.read_ctrl()
-        res = {"value": round(world * n ** 3 * c.numsteps / secs * 1e-9, 4),
-               "ms_per_step": round(secs / steps * 1e3, 3), "accepted_steps": int(c.numsteps),
-               "status": int(c.status)}
-        del dev
     out = {"workload": f"acoustics_3d_pulse {n}^3, wall BCs, MC, transverse_waves 22 "
-                       f"(corner transport), CFL 0.9, FP64, {steps} steps",
-           "unit": UNIT, "fp64": res, "launches": 9 * (steps + 3)}
+                       f"(corner transport), CFL 0.9, {steps} steps",
+           "unit": UNIT, "launches": 2 * 9 * (steps + 3)}
+    finals = {}
+    for name, prec in (("fp64", 0), ("fp32_bulk", 1)):
+        for prob, k in ((workloads.acoustics_3d_pulse(32), 3),
+                        (workloads.acoustics_3d_pulse(n), steps)):
+            dev = DeviceProblem3(prob.solver_struct(precision=prec), device=device)
+            dev.upload(prob.q0)
+            dev.ctrl_init(0.0, prob.dt_initial, math.inf, cfl_max=prob.cfl_max,
+                          cfl_desired=prob.cfl_desired, max_accepted=k, max_steps=10 * k)
+            torch.cuda.synchronize()
+            barrier(world)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dev.advance(k)
+            e1.record()
+            torch.cuda.synchronize()
+            secs = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world, device)
+            c = dev.read_ctrl()
+        out[name] = {"value": round(world * n ** 3 * c.numsteps / secs * 1e-9, 4),
+                     "ms_per_step": round(secs / steps * 1e3, 3),
+                     "accepted_steps": int(c.numsteps), "status": int(c.status)}
+        finals[name] = dev.q[c.parity].clone()
+        del dev
+    a, b = finals["fp32_bulk"], finals["fp64"]
+    out["fp32_rel_l1_vs_fp64"] = float((a - b).abs().sum() / b.abs().sum())
     if int(os.environ.get("RANK", "0")) == 0:
         from oracle import ref
         small = workloads.acoustics_3d_pulse(48)

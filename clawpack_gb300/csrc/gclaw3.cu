@@ -36,7 +36,7 @@ struct Args3 {
     const double *qin[2];
     double *qout[2];
     gclaw_ctrl *ctrl;
-    double *ws;
+    void *ws;  // edge records, in the arithmetic type of the step
     double dt, d[3];
     int n[3];
     int bc_lo[3], bc_hi[3];
@@ -220,18 +220,17 @@ __device__ __forceinline__ Launch launch_state(const Args3 &a) {
 }
 
 // ---- k_edges: normal Riemann problems ---------------------------------------
-template <template <typename> class RPT, int D>
-__global__ void __launch_bounds__(NT3) k_edges(const Args3 a,
-                                               const typename RPT<double>::Params P) {
-    using RP = RPT<double>;
+template <template <typename> class RPT, int D, typename T>
+__global__ void __launch_bounds__(NT3) k_edges(const Args3 a, const typename RPT<T>::Params P) {
+    using RP = RPT<T>;
     using F = Fields<RP>;
     constexpr int M = RP::M, MW = RP::MW;
     constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
     const Launch L = launch_state(a);
     if (L.skip) return;
     const double *__restrict__ qin = a.qin[L.par];
-    const double dtdn = L.dt / a.d[D];
-    double cmax = 0.0;
+    const T dtdn = (T)(L.dt / a.d[D]);
+    T cmax = (T)0;
     bool bad = false;
     const long long idx = (long long)blockIdx.x * NT3 + threadIdx.x;
     if (idx < a.npos) {
@@ -242,15 +241,15 @@ __global__ void __launch_bounds__(NT3) k_edges(const Args3 a,
         p[2] = (int)(idx / ((long long)X * Y)) - 1;
         int l[3] = {p[0], p[1], p[2]};
         l[D] -= 1;
-        double ql[M], qr[M];
+        T ql[M], qr[M];
 #pragma unroll
         for (int k = 0; k < M; k++) {
-            ql[k] = load_q3<M>(a, qin, k, l[0], l[1], l[2]);
-            qr[k] = load_q3<M>(a, qin, k, p[0], p[1], p[2]);
+            ql[k] = from_double<T>(load_q3<M>(a, qin, k, l[0], l[1], l[2]));
+            qr[k] = from_double<T>(load_q3<M>(a, qin, k, p[0], p[1], p[2]));
         }
-        double W[MW * M], s[MW], am[M], ap[M];
+        T W[MW * M], s[MW], am[M], ap[M];
         RP::template rpn3<D>(P, ql, qr, W, s, am, ap);
-        double *ws = a.ws;
+        T *ws = static_cast<T *>(a.ws);
         const long long np = a.npos;
 #pragma unroll
         for (int f = 0; f < MW * M; f++) ws[(F::W + f) * np + idx] = W[f];
@@ -272,54 +271,52 @@ __global__ void __launch_bounds__(NT3) k_edges(const Args3 a,
         }
     }
     // block max and flag, then one atomic each
-    __shared__ double s_red[NT3 / 32];
+    __shared__ T s_red[NT3 / 32];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) cmax = fmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
+    for (int off = 16; off > 0; off >>= 1) cmax = tmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
     if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = cmax;
     const int any = __syncthreads_or(bad ? 1 : 0);
     if (threadIdx.x == 0) {
-        for (int w = 1; w < NT3 / 32; w++) cmax = fmax(cmax, s_red[w]);
-        if (cmax > 0.0)
-            atomicMax(&a.ctrl->smax_bits[0], (unsigned long long)__double_as_longlong(cmax));
+        for (int w = 1; w < NT3 / 32; w++) cmax = tmax(cmax, s_red[w]);
+        const double c = (double)cmax;
+        if (c > 0.0) atomicMax(&a.ctrl->smax_bits[0], (unsigned long long)__double_as_longlong(c));
         if (any) atomicOr(&a.ctrl->flags, 1u);
     }
 }
 
 // ---- k_chains: limiter, correction flux, transverse chains -----------------
-template <class RP, int D>
-__device__ __forceinline__ void chain(const typename RP::Params &P, const double *asdq,
-                                      bool dbl, double h, double f1, double f2, double *ws,
-                                      long long np, long long idx, int base) {
-    using F = Fields<RP>;
+template <class RP, int D, typename T>
+__device__ __forceinline__ void chain(const typename RP::Params &P, const T *asdq, bool dbl, T h,
+                                      T f1, T f2, T *ws, long long np, long long idx, int base) {
     constexpr int M = RP::M;
     constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
-    double bm[M], bp[M], cm[M], cp[M];
+    T bm[M], bp[M], cm[M], cp[M];
     RP::template rpt3<T1>(P, asdq, bm, bp);
     RP::template rpt3<T2>(P, asdq, cm, cp);
-    double g[2][3][M], hh[2][3][M];
+    T g[2][3][M], hh[2][3][M];
 #pragma unroll
     for (int s = 0; s < 2; s++)
 #pragma unroll
         for (int o = 0; o < 3; o++)
 #pragma unroll
-            for (int k = 0; k < M; k++) g[s][o][k] = hh[s][o][k] = 0.0;
+            for (int k = 0; k < M; k++) g[s][o][k] = hh[s][o][k] = (T)0;
 #pragma unroll
     for (int k = 0; k < M; k++) {
-        g[0][1][k] = 0.0 - h * bm[k];
-        g[1][1][k] = 0.0 - h * bp[k];
-        hh[0][1][k] = 0.0 - h * cm[k];
-        hh[1][1][k] = 0.0 - h * cp[k];
+        g[0][1][k] = (T)0 - h * bm[k];
+        g[1][1][k] = (T)0 - h * bp[k];
+        hh[0][1][k] = (T)0 - h * cm[k];
+        hh[1][1][k] = (T)0 - h * cp[k];
     }
     if (dbl) {
-        double cmb[M], cpb[M];
+        T cmb[M], cpb[M];
 #pragma unroll
         for (int s = 0; s < 2; s++) {
             RP::template rptt3<T1, T2>(P, s ? bp : bm, cmb, cpb);
 #pragma unroll
             for (int k = 0; k < M; k++) {
                 g[s][1][k] = g[s][1][k] + f2 * (cpb[k] - cmb[k]);
-                g[s][2][k] = 0.0 - f2 * cpb[k];
-                g[s][0][k] = 0.0 + f2 * cmb[k];
+                g[s][2][k] = (T)0 - f2 * cpb[k];
+                g[s][0][k] = (T)0 + f2 * cmb[k];
             }
         }
 #pragma unroll
@@ -328,8 +325,8 @@ __device__ __forceinline__ void chain(const typename RP::Params &P, const double
 #pragma unroll
             for (int k = 0; k < M; k++) {
                 hh[s][1][k] = hh[s][1][k] + f1 * (cpb[k] - cmb[k]);
-                hh[s][2][k] = 0.0 - f1 * cpb[k];
-                hh[s][0][k] = 0.0 + f1 * cmb[k];
+                hh[s][2][k] = (T)0 - f1 * cpb[k];
+                hh[s][0][k] = (T)0 + f1 * cmb[k];
             }
         }
     }
@@ -346,10 +343,9 @@ __device__ __forceinline__ void chain(const typename RP::Params &P, const double
             }
 }
 
-template <template <typename> class RPT, int D>
-__global__ void __launch_bounds__(NT3) k_chains(const Args3 a,
-                                                const typename RPT<double>::Params P) {
-    using RP = RPT<double>;
+template <template <typename> class RPT, int D, typename T>
+__global__ void __launch_bounds__(NT3) k_chains(const Args3 a, const typename RPT<T>::Params P) {
+    using RP = RPT<T>;
     using F = Fields<RP>;
     constexpr int M = RP::M, MW = RP::MW;
     constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
@@ -364,30 +360,30 @@ __global__ void __launch_bounds__(NT3) k_chains(const Args3 a,
     p[2] = (int)(idx / ((long long)X * Y)) - 1;
     // edges 0..n along the sweep, slices -1..n across it
     if (p[D] < 0 || p[D] > a.n[D] || p[T1] > a.n[T1] || p[T2] > a.n[T2]) return;
-    double *ws = a.ws;
+    T *ws = static_cast<T *>(a.ws);
     const long long np = a.npos;
     long long stepd = 1;
     if (D >= 1) stepd *= X;
     if (D >= 2) stepd *= Y;
-    const double dtdn = L.dt / a.d[D], dtt1 = L.dt / a.d[T1], dtt2 = L.dt / a.d[T2];
+    const T dtdn = (T)(L.dt / a.d[D]), dtt1 = (T)(L.dt / a.d[T1]), dtt2 = (T)(L.dt / a.d[T2]);
 
-    double W[MW * M], s[MW], cq[M];
+    T W[MW * M], s[MW], cq[M];
 #pragma unroll
     for (int f = 0; f < MW * M; f++) W[f] = ws[(F::W + f) * np + idx];
 #pragma unroll
     for (int q = 0; q < MW; q++) s[q] = ws[(F::S + q) * np + idx];
 #pragma unroll
-    for (int k = 0; k < M; k++) cq[k] = 0.0;
+    for (int k = 0; k < M; k++) cq[k] = (T)0;
     if (a.order == 2) {
 #pragma unroll
         for (int q = 0; q < MW; q++) {
             const int lim = (a.mthlim >> (8 * q)) & 0xff;
             if (lim == 0) continue;
-            double wn2 = 0.0;
+            T wn2 = (T)0;
 #pragma unroll
             for (int k = 0; k < M; k++) wn2 = wn2 + W[q * M + k] * W[q * M + k];
             if (eq0(wn2)) continue;
-            double dot = 0.0;
+            T dot = (T)0;
             if (gt0(s[q])) {  // upwind: the edge before
 #pragma unroll
                 for (int k = 0; k < M; k++)
@@ -397,32 +393,32 @@ __global__ void __launch_bounds__(NT3) k_chains(const Args3 a,
                 for (int k = 0; k < M; k++)
                     dot = dot + W[q * M + k] * ws[(F::W + q * M + k) * np + idx + stepd];
             }
-            double phi = 0.0;
+            T phi = (T)0;
             if (!le0(dot)) {
-                const double th = dot / wn2;
-                phi = gt0(th) ? philim_pos<double>(lim, th) : philim<double>(lim, th);
+                const T th = qdiv(dot, wn2);
+                phi = gt0(th) ? philim_pos<T>(lim, th) : philim<T>(lim, th);
             }
 #pragma unroll
             for (int k = 0; k < M; k++) W[q * M + k] = phi * W[q * M + k];
         }
-        const double dtave = 0.5 * (dtdn + dtdn);
+        const T dtave = (T)0.5 * (dtdn + dtdn);
 #pragma unroll
         for (int k = 0; k < M; k++) {
-            double c = 0.0;
+            T c = (T)0;
 #pragma unroll
             for (int q = 0; q < MW; q++) {
-                const double sa = fabs(s[q]);
-                c = c + sa * (1.0 - sa * dtave) * W[q * M + k];
+                const T sa = tabs(s[q]);
+                c = c + sa * ((T)1 - sa * dtave) * W[q * M + k];
             }
             cq[k] = c;
         }
     }
 #pragma unroll
-    for (int k = 0; k < M; k++) ws[(F::FA + k) * np + idx] = 0.0 + 0.5 * cq[k];
+    for (int k = 0; k < M; k++) ws[(F::FA + k) * np + idx] = (T)0 + (T)0.5 * cq[k];
 
     const int single = a.tw / 10;
     const bool dbl = (a.tw % 10) > 0;
-    double am[M], ap[M];
+    T am[M], ap[M];
 #pragma unroll
     for (int k = 0; k < M; k++) {
         am[k] = ws[(F::AM + k) * np + idx];
@@ -433,27 +429,31 @@ __global__ void __launch_bounds__(NT3) k_chains(const Args3 a,
         }
     }
     if (single > 0) {
-        const double h = 0.5 * dtdn;
-        const double sixth = 1.0 / 6.0;
-        const double f1 = sixth * dtdn * dtt1, f2 = sixth * dtdn * dtt2;
-        chain<RP, D>(P, am, dbl, h, f1, f2, ws, np, idx, F::AMC);
-        chain<RP, D>(P, ap, dbl, h, f1, f2, ws, np, idx, F::APC);
+        const T h = (T)0.5 * dtdn;
+        const T sixth = (T)(1.0 / 6.0);
+        const T f1 = sixth * dtdn * dtt1, f2 = sixth * dtdn * dtt2;
+        chain<RP, D, T>(P, am, dbl, h, f1, f2, ws, np, idx, F::AMC);
+        chain<RP, D, T>(P, ap, dbl, h, f1, f2, ws, np, idx, F::APC);
     } else {
 #pragma unroll
         for (int e = 0; e < F::NCH; e++) {
-            ws[(long long)(F::AMC + e) * np + idx] = 0.0;
-            ws[(long long)(F::APC + e) * np + idx] = 0.0;
+            ws[(long long)(F::AMC + e) * np + idx] = (T)0;
+            ws[(long long)(F::APC + e) * np + idx] = (T)0;
         }
     }
 }
 
 // ---- k_update: per-cell accumulation of one sweep ---------------------------
-template <template <typename> class RPT, int D>
+// FP64: the terms are added to the state itself, in the oracle's order.
+// FP32-bulk: they are summed in FP32 from zero and the sum is added to the
+// FP64 state once.
+template <template <typename> class RPT, int D, typename T>
 __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
-    using RP = RPT<double>;
+    using RP = RPT<T>;
     using F = Fields<RP>;
     constexpr int M = RP::M;
     constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+    constexpr bool F64 = sizeof(T) == 8;
     const Launch L = launch_state(a);
     if (L.skip) return;
     const long long ncell = (long long)a.n[0] * a.n[1] * a.n[2];
@@ -467,12 +467,12 @@ __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
         const double *src = D == 0 ? a.qin[L.par] : a.qout[L.par];
         double *dst = a.qout[L.par];
         const size_t o = (size_t)M * (size_t)cid;
-        const double *ws = a.ws;
+        const T *ws = static_cast<const T *>(a.ws);
         const long long np = a.npos;
-        const double dtn = L.dt / a.d[D], dt1 = L.dt / a.d[T1], dt2 = L.dt / a.d[T2];
-        double v[M];
+        const T dtn = (T)(L.dt / a.d[D]), dt1 = (T)(L.dt / a.d[T1]), dt2 = (T)(L.dt / a.d[T2]);
+        T v[M];
 #pragma unroll
-        for (int k = 0; k < M; k++) v[k] = src[o + k];
+        for (int k = 0; k < M; k++) v[k] = F64 ? (T)src[o + k] : (T)0;
         const int c = p[D], A = p[T1], B = p[T2];
 #pragma unroll
         for (int db = -1; db <= 1; db++)
@@ -486,36 +486,37 @@ __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
                 const long long i1 = bpos(a, e1[0], e1[1], e1[2]);
                 // flux entry (part, face s, offset o) of this slice at cell c
                 // (entries that cannot be nonzero are +0, as stored by the oracle)
-                auto ent = [&](int part, int s, int off, int k) {
+                auto ent = [&](int part, int s, int off, int k) -> T {
                     const int slot = chain_slot<RP, D>(part, s, off + 1, k);
-                    if (slot < 0) return (0.0 + 0.0) + 0.0;
-                    const double am = ws[(long long)(F::AMC + slot) * np + i1];
-                    const double ap = ws[(long long)(F::APC + slot) * np + i0];
-                    return (0.0 + am) + ap;
+                    if (slot < 0) return ((T)0 + (T)0) + (T)0;
+                    const T am = ws[(long long)(F::AMC + slot) * np + i1];
+                    const T ap = ws[(long long)(F::APC + slot) * np + i0];
+                    return ((T)0 + am) + ap;
                 };
 #pragma unroll
                 for (int k = 0; k < M; k++) {
                     if (da == 0 && db == 0) {
-                        const double qa = (0.0 - dtn * ws[(F::AP + k) * np + i0]) -
-                                          dtn * ws[(F::AM + k) * np + i1];
-                        const double fa0 = ws[(F::FA + k) * np + i0];
-                        const double fa1 = ws[(F::FA + k) * np + i1];
+                        const T qa = ((T)0 - dtn * ws[(F::AP + k) * np + i0]) -
+                                     dtn * ws[(F::AM + k) * np + i1];
+                        const T fa0 = ws[(F::FA + k) * np + i0];
+                        const T fa1 = ws[(F::FA + k) * np + i1];
                         v[k] = v[k] + qa - dtn * (fa1 - fa0) -
                                dt1 * (ent(0, 1, 0, k) - ent(0, 0, 0, k)) -
                                dt2 * (ent(1, 1, 0, k) - ent(1, 0, 0, k));
                     } else {
-                        const double gt = da == 0 ? 0.0 - dt1 * (ent(0, 1, db, k) - ent(0, 0, db, k))
-                                          : da == 1 ? dt1 * ent(0, 1, db, k)
-                                                    : 0.0 - dt1 * ent(0, 0, db, k);
-                        const double ht = db == 0 ? 0.0 - dt2 * (ent(1, 1, da, k) - ent(1, 0, da, k))
-                                          : db == 1 ? dt2 * ent(1, 1, da, k)
-                                                    : 0.0 - dt2 * ent(1, 0, da, k);
+                        const T gt = da == 0 ? (T)0 - dt1 * (ent(0, 1, db, k) - ent(0, 0, db, k))
+                                     : da == 1 ? dt1 * ent(0, 1, db, k)
+                                               : (T)0 - dt1 * ent(0, 0, db, k);
+                        const T ht = db == 0 ? (T)0 - dt2 * (ent(1, 1, da, k) - ent(1, 0, da, k))
+                                     : db == 1 ? dt2 * ent(1, 1, da, k)
+                                               : (T)0 - dt2 * ent(1, 0, da, k);
                         v[k] = v[k] + gt + ht;
                     }
                 }
             }
 #pragma unroll
-        for (int k = 0; k < M; k++) dst[o + k] = v[k];
+        for (int k = 0; k < M; k++)
+            dst[o + k] = F64 ? (double)v[k] : src[o + k] + f2d_bits((float)v[k]);
     }
     if (D == 2) {
         // last block of the step: Courant number and evolve_to_time rules
@@ -534,27 +535,34 @@ __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
     }
 }
 
-template <template <typename> class RPT, int D>
+template <template <typename> class RPT, int D, typename T>
 static int sweep(const gclaw3_solver *s, const Args3 &a, cudaStream_t st) {
-    const typename RPT<double>::Params P = RPT<double>::make(s->problem_data);
+    const typename RPT<T>::Params P = RPT<T>::make(s->problem_data);
     const unsigned nb = (unsigned)((a.npos + NT3 - 1) / NT3);
     const long long ncell = (long long)s->mx * s->my * s->mz;
     const unsigned nc = (unsigned)((ncell + NT3 - 1) / NT3);
-    k_edges<RPT, D><<<nb, NT3, 0, st>>>(a, P);
-    k_chains<RPT, D><<<nb, NT3, 0, st>>>(a, P);
-    k_update<RPT, D><<<nc, NT3, 0, st>>>(a);
+    k_edges<RPT, D, T><<<nb, NT3, 0, st>>>(a, P);
+    k_chains<RPT, D, T><<<nb, NT3, 0, st>>>(a, P);
+    k_update<RPT, D, T><<<nc, NT3, 0, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
 }
 
-template <template <typename> class RPT>
-static int step_all(const gclaw3_solver *s, const Args3 &a, cudaStream_t st, int nsteps) {
+template <template <typename> class RPT, typename T>
+static int step_all_t(const gclaw3_solver *s, const Args3 &a, cudaStream_t st, int nsteps) {
     for (int n = 0; n < nsteps; n++) {
-        int rc = sweep<RPT, 0>(s, a, st);
-        if (!rc) rc = sweep<RPT, 1>(s, a, st);
-        if (!rc) rc = sweep<RPT, 2>(s, a, st);
+        int rc = sweep<RPT, 0, T>(s, a, st);
+        if (!rc) rc = sweep<RPT, 1, T>(s, a, st);
+        if (!rc) rc = sweep<RPT, 2, T>(s, a, st);
         if (rc) return rc;
     }
     return GCLAW_OK;
+}
+
+// FP64, or FP32 edge records and fluxes with the FP64 state (FP32-bulk).
+template <template <typename> class RPT>
+static int step_all(const gclaw3_solver *s, const Args3 &a, cudaStream_t st, int nsteps) {
+    return s->precision == GCLAW_PREC_FP64 ? step_all_t<RPT, double>(s, a, st, nsteps)
+                                           : step_all_t<RPT, float>(s, a, st, nsteps);
 }
 
 static long long box_positions(const gclaw3_solver *s) {
@@ -614,14 +622,16 @@ int gclaw3_check(const gclaw3_solver *s) {
     if (s->order < 1 || s->order > 2) return GCLAW_ERR_ARG;
     const int tw = s->transverse_waves;
     if (tw != 0 && tw != 10 && tw != 11 && tw != 20 && tw != 22) return GCLAW_ERR_UNSUPPORTED;
-    if (s->precision != GCLAW_PREC_FP64) return GCLAW_ERR_UNSUPPORTED;
+    if (s->precision != GCLAW_PREC_FP64 && s->precision != GCLAW_PREC_FP32_BULK)
+        return GCLAW_ERR_UNSUPPORTED;
     if (!(s->problem_data[2] > 0.0) || !(s->problem_data[3] > 0.0)) return GCLAW_ERR_ARG;
     return GCLAW_OK;
 }
 
 size_t gclaw3_workspace_bytes(const gclaw3_solver *s) {
     if (gclaw3_check(s)) return 0;
-    return sizeof(double) * (size_t)Fields<Rp3Acoustics<double>>::NF * (size_t)box_positions(s);
+    const size_t elem = s->precision == GCLAW_PREC_FP64 ? sizeof(double) : sizeof(float);
+    return elem * (size_t)Fields<Rp3Acoustics<double>>::NF * (size_t)box_positions(s);
 }
 
 int gclaw3_step(const gclaw3_solver *s, const double *q_dev, double *qnew_dev, double dt,
@@ -638,7 +648,7 @@ int gclaw3_step(const gclaw3_solver *s, const double *q_dev, double *qnew_dev, d
     a.qin[0] = a.qin[1] = q_dev;
     a.qout[0] = a.qout[1] = qnew_dev;
     a.ctrl = ctrl_dev;
-    a.ws = (double *)ws_dev;
+    a.ws = ws_dev;
     a.dt = dt;
     a.ctrl_mode = 0;
     return step_all<Rp3Acoustics>(s, a, st, 1);
@@ -657,7 +667,7 @@ int gclaw3_advance(const gclaw3_solver *s, double *q0_dev, double *q1_dev, void 
     a.qout[0] = q1_dev;
     a.qout[1] = q0_dev;
     a.ctrl = ctrl_dev;
-    a.ws = (double *)ws_dev;
+    a.ws = ws_dev;
     a.dt = 0.0;
     a.ctrl_mode = 1;
     return step_all<Rp3Acoustics>(s, a, (cudaStream_t)stream, nsteps);

@@ -35,6 +35,10 @@
 namespace gclaw {
 
 template <typename T>
+__device__ __forceinline__ T tabs(T a) { return fabs(a); }
+template <>
+__device__ __forceinline__ float tabs<float>(float a) { return fabsf(a); }
+template <typename T>
 __device__ __forceinline__ T tmin(T a, T b) { return fmin(a, b); }
 template <typename T>
 __device__ __forceinline__ T tmax(T a, T b) { return fmax(a, b); }

@@ -378,8 +378,8 @@ class ClawSolver3D(ClawSolver2D):
     ``transverse_waves`` takes ClawSolver3D's values: 0, 10 / 11
     (``trans_inc``: transverse propagation of the increment waves, without /
     with the corner terms) and 20 / 22 (``trans_cor``: also of the correction
-    waves).  Steps are unsplit (``dimensional_split = False``), FP64, without
-    aux arrays."""
+    waves).  Steps are unsplit (``dimensional_split = False``), without aux
+    arrays, in FP64 or FP32-bulk (``precision``)."""
     no_trans = 0
     trans_inc = 11
     trans_cor = 22
@@ -427,8 +427,8 @@ class ClawSolver3D(ClawSolver2D):
                 raise ValueError("boundary conditions are not set")
             if b == BC.custom:
                 raise NotImplementedError("BC.custom is not supported by the CUDA backend")
-        if self.precision != "fp64":
-            raise NotImplementedError("3D steps are FP64 (solver.precision = 'fp64')")
+        if self.precision not in ("fp64", "fp32"):
+            raise ValueError("solver.precision must be 'fp64' or 'fp32'")
         if self.step_source is not None and self.source_split not in (1, 2):
             raise ValueError("solver.source_split must be 1 (Godunov) or 2 (Strang)")
 
@@ -440,8 +440,9 @@ class ClawSolver3D(ClawSolver2D):
         dx, dy, dz = g.delta
         return make_solver3_struct(self.rp.rp_id, mx, my, mz, dx, dy, dz, self.bc_lower,
                                    self.bc_upper, self._mthlim, self.order,
-                                   self.transverse_waves, _lib.PREC_FP64,
-                                   self._problem_data(state))
+                                   self.transverse_waves,
+                                   _lib.PREC_FP64 if self.precision == "fp64"
+                                   else _lib.PREC_FP32_BULK, self._problem_data(state))
 
     def _device(self, state):
         s = self.solver_struct(state)

@@ -85,7 +85,7 @@ def run_3d(a):
     from .device import DeviceProblem3
 
     w = workloads.acoustics_3d_pulse(a.mx)
-    dev = DeviceProblem3(w.solver_struct())
+    dev = DeviceProblem3(w.solver_struct(precision=0 if a.precision == "fp64" else 1))
     dev.upload(w.q0)
     dev.ctrl_init(0.0, w.dt_initial, math.inf, cfl_max=w.cfl_max, cfl_desired=w.cfl_desired,
                   max_steps=10 ** 9)
@@ -98,7 +98,7 @@ def run_3d(a):
     c = dev.read_ctrl()
     ms = e0.elapsed_time(e1) / max(a.steps, 1)
     cells = w.n ** 3
-    print(json.dumps({"workload": w.name, "n": w.n, "precision": "fp64", "steps": a.steps,
+    print(json.dumps({"workload": w.name, "n": w.n, "precision": a.precision, "steps": a.steps,
                       "ms_per_step": ms,
                       "gcell_updates_per_s": cells / (ms * 1e-3) * 1e-9 if ms > 0 else None,
                       "accepted": c.numsteps, "status": c.status, "cfl": c.cfl}))

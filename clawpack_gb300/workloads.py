@@ -337,12 +337,12 @@ class Workload3:
     cfl_desired: float = 0.9
     cfl_max: float = 1.0
 
-    def solver_struct(self, order=2, tw=22, lim=tvd.MC):
+    def solver_struct(self, order=2, tw=22, lim=tvd.MC, precision=_lib.PREC_FP64):
         from .device import make_solver3_struct
 
         return make_solver3_struct(_lib.RP3_ACOUSTICS_3D, self.n, self.n, self.n, *self.delta,
                                    self.bc_lower, self.bc_upper, [lim, lim], order, tw,
-                                   _lib.PREC_FP64, self.problem_data)
+                                   precision, self.problem_data)
 
 
 def acoustics_3d_pulse(n=192):

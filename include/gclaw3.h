@@ -37,14 +37,15 @@ typedef struct gclaw3_solver {
     int mthlim[GCLAW_MAX_WAVES];  /* limiter per wave family */
     int order;                    /* 1 or 2 */
     int transverse_waves;         /* 0, 10, 11, 20 or 22 (ClawSolver3D: 22) */
-    int precision;                /* GCLAW_PREC_FP64 */
+    int precision;                /* GCLAW_PREC_FP64, or GCLAW_PREC_FP32_BULK: FP32 edge
+                                     records and fluxes, FP64 state */
     double problem_data[8];
 } gclaw3_solver;
 
 int gclaw3_rp_shape(int rp, int *num_eqn, int *num_waves);
 
 /* 0 if the description can be stepped, else GCLAW_ERR_ARG or
- * GCLAW_ERR_UNSUPPORTED (FP32, unknown transverse option). */
+ * GCLAW_ERR_UNSUPPORTED (unknown transverse option or precision). */
 int gclaw3_check(const gclaw3_solver *s);
 
 /* Bytes of device workspace a step of this grid needs. */

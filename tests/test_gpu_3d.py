@@ -4,9 +4,9 @@ GPU against the oracle's restatement of classic3.
 The -fmad=false build must reproduce the oracle bit for bit for every
 transverse option (0, 10, 11, 20, 22), order, limiter and boundary mix,
 including grids of 2 cells in a direction; the product build stays within
-1e-13 per step; device-controlled time stepping follows the oracle's
-evolve_to_time within 1e-12; FP32 and unknown transverse options are
-refused."""
+1e-13 per step and FP32-bulk within 2e-6; device-controlled time stepping
+follows the oracle's evolve_to_time within 1e-12 (FP64) and 1e-6 (FP32);
+unknown transverse options and precisions are refused."""
 import ctypes
 import math
 
@@ -21,9 +21,9 @@ pytestmark = pytest.mark.gpu
 PD3 = [1.0, 4.0, 2.0, 2.0]
 
 
-def gpu_step3(q, d, dt, bcl, bcu, order=2, tw=22, lim=4, strict=False):
+def gpu_step3(q, d, dt, bcl, bcu, order=2, tw=22, lim=4, strict=False, precision=0):
     m, mx, my, mz = q.shape
-    s = make_solver3_struct(1, mx, my, mz, *d, bcl, bcu, [lim] * 2, order, tw, 0, PD3)
+    s = make_solver3_struct(1, mx, my, mz, *d, bcl, bcu, [lim] * 2, order, tw, precision, PD3)
     dev = DeviceProblem3(s, strict=strict)
     dev.upload(q)
     dev.step(dt, src=0)
@@ -51,6 +51,8 @@ def test_strict_bitwise(cuda, oracle, shape, bcl, bcu):
     assert c.cfl == cflo
     qp, cp = gpu_step3(q, d, dt, bcl, bcu, lim=lim)
     assert rel_l1(qp, qo) <= 1e-13 and abs(cp.cfl - cflo) <= 1e-14 * cflo
+    q32, c32 = gpu_step3(q, d, dt, bcl, bcu, lim=lim, precision=1)
+    assert rel_l1(q32, qo) <= 2e-6 and abs(c32.cfl - cflo) <= 1e-6 * cflo
 
 
 @pytest.mark.parametrize("order,tw,lim", [(2, 22, 4), (2, 20, 2), (2, 11, 3), (1, 10, 0),
@@ -101,10 +103,14 @@ def test_refusals(cuda):
     s = make_solver3_struct(1, 8, 8, 8, 0.1, 0.1, 0.1, [1] * 3, [1] * 3, [4, 4], 2, 21, 0, PD3)
     assert L.gclaw3_check(ctypes.byref(s)) == _lib.ERR_UNSUPPORTED
     s.transverse_waves = 22
-    s.precision = 1
+    s.precision = 2
     assert L.gclaw3_check(ctypes.byref(s)) == _lib.ERR_UNSUPPORTED
+    s.precision = 1  # FP32-bulk: half the workspace
+    assert L.gclaw3_check(ctypes.byref(s)) == 0
+    b32 = L.gclaw3_workspace_bytes(ctypes.byref(s))
     s.precision = 0
     assert L.gclaw3_check(ctypes.byref(s)) == 0
+    assert L.gclaw3_workspace_bytes(ctypes.byref(s)) == 2 * b32
     s.mz = 1
     assert L.gclaw3_check(ctypes.byref(s)) == _lib.ERR_ARG
 
@@ -140,3 +146,25 @@ def test_controller_run_through_clawsolver3d(cuda, oracle):
     for k in range(1, 4):
         q, t, dt, _ = oracle.evolve(step, q, t, 0.1 * k, dt, cfl_desired=0.9, cfl_max=1.0)
         assert rel_l1(claw.frames[k].q, q) <= 1e-12, k
+
+
+def test_fp32_bulk_evolve(cuda, oracle):
+    mx, my, mz = 24, 20, 16
+    x = (np.arange(mx) + 0.5) / mx - 0.5
+    y = (np.arange(my) + 0.5) / my - 0.5
+    z = (np.arange(mz) + 0.5) / mz - 0.5
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    q = np.zeros((4, mx, my, mz), order="F")
+    q[0] = np.exp(-40.0 * (X ** 2 + Y ** 2 + Z ** 2))
+    d = (1.0 / mx, 1.0 / my, 1.0 / mz)
+    bc = [3, 3, 3]
+    res = {}
+    for prec in (0, 1):
+        s = make_solver3_struct(1, mx, my, mz, *d, bc, bc, [4, 4], 2, 22, prec, PD3)
+        dev = DeviceProblem3(s)
+        dev.upload(q)
+        c = dev.evolve(0.0, 0.002, 0.3, cfl_max=1.0, cfl_desired=0.9)
+        assert c.status == 0
+        res[prec] = (dev.download(c.parity), c)
+    assert res[0][1].numsteps == res[1][1].numsteps
+    assert rel_l1(res[1][0], res[0][0]) <= 1e-6
