@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(NT, tile_min_blocks<T, NT>()) step_kernel(cons
 
     T smax_x = (T)0, smax_y = (T)0;
     bool bad = false;
-    step_tile<RPT, T, TX, TY, NT>(a, P, qin, qout, dtdx, dtdy, blockIdx.x * TX, blockIdx.y * TY,
+    step_tile<RPT, T, TX, TY, NT>(a, P, qin, qout, dtdx, dtdy, blockIdx.x * TX,
+                                  (blockIdx.y + a.ty0) * TY,
                                   smem_raw, smax_x, smax_y, bad);
 
     const int anybad = block_reduce<T, NT>(smax_x, smax_y, bad, s_red);
@@ -206,7 +207,7 @@ static int launch_tile(const gclaw_solver *s, const StepArgs &a, cudaStream_t st
         if (dev < 32) configured_mask |= (1 << dev);
     }
     const typename RP::Params P = RP::make(s->problem_data);
-    dim3 grid((s->mx + TX - 1) / TX, (s->my + TY - 1) / TY);
+    dim3 grid((s->mx + TX - 1) / TX, a.nty > 0 ? a.nty : (s->my + TY - 1) / TY);
     for (int l = 0; l < nlaunch; l++) kern<<<grid, NT, smem, st>>>(a, P);
     return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
 }
@@ -346,6 +347,116 @@ static void fill_args(const gclaw_solver *s, StepArgs &a) {
         a.abc_lo[d] = s->aux_bc_lower[d];
         a.abc_hi[d] = s->aux_bc_upper[d];
     }
+}
+
+// ---- host-buffer step, band by band ------------------------------------------
+// gclaw_step_host moves a whole state each way every step.  For the FP64
+// tile kernel the step is launched as GCLAW_HOST_BANDS bands of tile rows on
+// the caller's stream while a copy stream moves the input rows in ahead of
+// the band that needs them (its rows and the two-row halo) and the output
+// rows of each finished band back, so the copies overlap the step except for
+// the first input band and the last output band.  Bands other than the last
+// leave the Courant reduction to the next (no_finish), so the result and the
+// Courant number are those of one launch.
+constexpr int GCLAW_HOST_BANDS = 4;
+
+struct HostPipe {
+    cudaStream_t copy;
+    cudaEvent_t start, in[GCLAW_HOST_BANDS], done[GCLAW_HOST_BANDS], out;
+    bool ready;
+};
+static HostPipe g_host_pipe[64];
+
+// The copy stream and events of the current device, created on first use.
+static int host_pipe(HostPipe **pp) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return GCLAW_ERR_CUDA;
+    HostPipe &p = g_host_pipe[dev];
+    if (!p.ready) {
+        if (cudaStreamCreateWithFlags(&p.copy, cudaStreamNonBlocking) != cudaSuccess)
+            return GCLAW_ERR_CUDA;
+        cudaEvent_t *evs[] = {&p.start, &p.out};
+        for (cudaEvent_t *e : evs)
+            if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess)
+                return GCLAW_ERR_CUDA;
+        for (int b = 0; b < GCLAW_HOST_BANDS; b++)
+            if (cudaEventCreateWithFlags(&p.in[b], cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&p.done[b], cudaEventDisableTiming) != cudaSuccess)
+                return GCLAW_ERR_CUDA;
+        p.ready = true;
+    }
+    *pp = &p;
+    return GCLAW_OK;
+}
+
+// Number of bands for this solver (1: one launch).  Banding needs the FP64
+// tile kernel (the strip kernels cut rows their own way) and no periodic y
+// boundary (whose halo rows come from the other end of the grid).
+static int host_bands(const gclaw_solver *s) {
+    if (s->precision != GCLAW_PREC_FP64 || g_fp64_kernel == 2 || s->capa) return 1;
+    if (s->bc_lower[1] == GCLAW_BC_PERIODIC) return 1;
+    int tx, ty;
+    tile_shape(s->rp, s->precision, &tx, &ty);
+    const int nty = (s->my + ty - 1) / ty;
+    return nty >= 2 * GCLAW_HOST_BANDS ? GCLAW_HOST_BANDS : 1;
+}
+
+static int step_host_banded(const gclaw_solver *s, const double *q_host, double *qnew_host,
+                            double dt, double *d_q, double *d_new, gclaw_ctrl *ws,
+                            cudaStream_t st, HostPipe *pp, int nband) {
+    int m, mw, tx, ty;
+    gclaw_rp_shape(s->rp, &m, &mw);
+    tile_shape(s->rp, s->precision, &tx, &ty);
+    const int nty = (s->my + ty - 1) / ty;
+    const size_t row = (size_t)m * (size_t)s->mx;  // doubles per row of cells
+    int t0[GCLAW_HOST_BANDS + 1];
+    for (int b = 0; b <= nband; b++) t0[b] = (int)((long long)nty * b / nband);
+    auto rows = [&](int b, size_t *off, size_t *n) {
+        const int r0 = t0[b] * ty, r1 = t0[b + 1] * ty < s->my ? t0[b + 1] * ty : s->my;
+        *off = row * (size_t)r0;
+        *n = row * (size_t)(r1 - r0);
+    };
+    // the copy stream starts after the work already on the caller's stream
+    if (cudaEventRecord(pp->start, st) != cudaSuccess ||
+        cudaStreamWaitEvent(pp->copy, pp->start, 0) != cudaSuccess)
+        return GCLAW_ERR_CUDA;
+    for (int b = 0; b < nband; b++) {
+        size_t off, n;
+        rows(b, &off, &n);
+        if (cudaMemcpyAsync(d_q + off, q_host + off, n * sizeof(double),
+                            cudaMemcpyHostToDevice, pp->copy) != cudaSuccess ||
+            cudaEventRecord(pp->in[b], pp->copy) != cudaSuccess)
+            return GCLAW_ERR_CUDA;
+    }
+    for (int b = 0; b < nband; b++) {
+        // band b reads up to two rows past its end: the next band's input
+        const int need = b + 1 < nband ? b + 1 : b;
+        if (cudaStreamWaitEvent(st, pp->in[need], 0) != cudaSuccess) return GCLAW_ERR_CUDA;
+        StepArgs a{};
+        fill_args(s, a);
+        a.qin[0] = a.qin[1] = d_q;
+        a.qout[0] = a.qout[1] = d_new;
+        a.ctrl = ws;
+        a.dt = dt;
+        a.ghosted = 0;
+        a.ctrl_mode = 0;
+        a.ty0 = t0[b];
+        a.nty = t0[b + 1] - t0[b];
+        a.no_finish = b + 1 < nband;
+        int rc = dispatch(s, a, st, 1);
+        if (rc) return rc;
+        size_t off, n;
+        rows(b, &off, &n);
+        if (cudaEventRecord(pp->done[b], st) != cudaSuccess ||
+            cudaStreamWaitEvent(pp->copy, pp->done[b], 0) != cudaSuccess ||
+            cudaMemcpyAsync(qnew_host + off, d_new + off, n * sizeof(double),
+                            cudaMemcpyDeviceToHost, pp->copy) != cudaSuccess)
+            return GCLAW_ERR_CUDA;
+    }
+    if (cudaEventRecord(pp->out, pp->copy) != cudaSuccess ||
+        cudaStreamWaitEvent(st, pp->out, 0) != cudaSuccess)
+        return GCLAW_ERR_CUDA;
+    return GCLAW_OK;
 }
 
 }  // namespace gclaw
@@ -622,15 +733,23 @@ int gclaw_step_host(const gclaw_solver *s, const double *q_host, double *qnew_ho
     cudaStream_t st = (cudaStream_t)stream;
     // the workspace is raw caller memory: clear the control block whose
     // reduction slots and block counter the step expects at zero
-    if (cudaMemsetAsync(ws, 0, sizeof(gclaw_ctrl), st) != cudaSuccess ||
-        cudaMemcpyAsync(d_q, q_host, qb, cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return GCLAW_ERR_CUDA;
-    rc = gclaw_step(s, d_q, d_new, dt, ws, stream);
-    if (rc) return rc;
+    if (cudaMemsetAsync(ws, 0, sizeof(gclaw_ctrl), st) != cudaSuccess) return GCLAW_ERR_CUDA;
+    HostPipe *pp = nullptr;
+    const int nband = host_bands(s);
+    if (nband > 1 && host_pipe(&pp) == GCLAW_OK) {
+        rc = step_host_banded(s, q_host, qnew_host, dt, d_q, d_new, ws, st, pp, nband);
+        if (rc) return rc;
+    } else {
+        if (cudaMemcpyAsync(d_q, q_host, qb, cudaMemcpyHostToDevice, st) != cudaSuccess)
+            return GCLAW_ERR_CUDA;
+        rc = gclaw_step(s, d_q, d_new, dt, ws, stream);
+        if (rc) return rc;
+        if (cudaMemcpyAsync(qnew_host, d_new, qb, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            return GCLAW_ERR_CUDA;
+    }
     double cfl = 0.0;
     int status = 0;
-    if (cudaMemcpyAsync(qnew_host, d_new, qb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(&cfl, &ws->cfl, sizeof(double), cudaMemcpyDeviceToHost, st) !=
+    if (cudaMemcpyAsync(&cfl, &ws->cfl, sizeof(double), cudaMemcpyDeviceToHost, st) !=
             cudaSuccess ||
         cudaMemcpyAsync(&status, &ws->status, sizeof(int), cudaMemcpyDeviceToHost, st) !=
             cudaSuccess ||

@@ -30,6 +30,8 @@ struct StepArgs {
     int sweeps;     // 1: x-sweep only, 2: y-sweep only (dimensional splitting); else both
     int no_finish;  // last block resets the block counter but leaves the CFL
                     // reduction to the next launch (first sweep of a split step)
+    int ty0, nty;   // tile rows [ty0, ty0 + nty) only (nty > 0): one band of a
+                    // step launched band by band; nty = 0: the whole grid
 };
 
 // Value of component k of qbc(gi, gj) for gi in [-2, mx+1], gj in [-2, my+1]

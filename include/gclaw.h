@@ -222,7 +222,10 @@ size_t gclaw_step_workspace_bytes(const gclaw_solver *s);
  * (upstream pyclaw/src/pyclaw/classic/solver.py), here replacing
  * _apply_bcs + step2.  Copies q_host (num_eqn, mx, my) to the device, runs
  * gclaw_step, copies the new state to qnew_host and the Courant number to
- * *cfl_out, then synchronises the stream.  ws_dev (caller-owned, 256-byte
+ * *cfl_out, then synchronises the stream.  FP64 tile steps of grids of at
+ * least eight tile rows without a periodic y boundary run band by band,
+ * with the row copies on an internal stream overlapping the bands (same
+ * result); host memory should be pinned for the copies to overlap.  ws_dev (caller-owned, 256-byte
  * aligned, at least gclaw_step_workspace_bytes, any contents) holds the
  * control block, which each call clears, and both device states. */
 int gclaw_step_host(const gclaw_solver *s, const double *q_host, double *qnew_host, double dt,

@@ -56,6 +56,32 @@ def test_step_host_with_dirty_workspace_is_bitwise(cuda, oracle, rp):
         qcur = out
 
 
+@pytest.mark.parametrize("rp", [1, 2, 3])
+@pytest.mark.parametrize("bcl,bcu", [([3, 1], [1, 3]), ([1, 2], [1, 2])])
+def test_step_host_bands_are_bitwise(cuda, oracle, rp, bcl, bcu):
+    """A grid tall enough for the band-by-band host step (FP64 tiles, copies
+    overlapping the bands): the same bits as the oracle in the strict build,
+    with a periodic y boundary (one launch) as well."""
+    mx, my = 70, 300
+    rng = np.random.default_rng(21 + rp)
+    q = np.asfortranarray(random_state(rp, mx, my, rng))
+    dx, dy = 1.0 / mx, 1.0 / my
+    dt = 0.05 * min(dx, dy)
+    s = make_solver_struct(rp, mx, my, dx, dy, bcl, bcu, [4] * SHAPES[rp][1], 2, 2, 0, PD[rp])
+    L = _lib.lib(strict=True)
+    nb = L.gclaw_step_workspace_bytes(ctypes.byref(s))
+    buf, base = aligned_workspace(nb, 0xFF)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    qo, cflo, rc = oracle.step(rp, PD[rp], q, dx, dy, dt, bcl, bcu, 2, 2, [4] * 4)
+    out = np.empty_like(q, order="F")
+    cfl = ctypes.c_double(-1.0)
+    status = L.gclaw_step_host(ctypes.byref(s), ptr(q), ptr(out), dt, ctypes.c_void_p(base), nb,
+                               ctypes.byref(cfl), stream)
+    assert status == 0
+    assert np.array_equal(out, qo)
+    assert cfl.value == cflo
+
+
 def test_evolve_host_matches_device_evolve(cuda):
     rp, mx, my = 2, 64, 40
     X, Y = np.meshgrid((np.arange(mx) + 0.5) / mx, (np.arange(my) + 0.5) / my, indexing="ij")
