@@ -10,8 +10,11 @@ Metric: Gcell-updates/s (interior cells x accepted steps / time).
   value    plain FP64 step, device-timed with CUDA events around each step
            kernel; the L2 is flushed (256 MB write) before every timed step.
   e2e      the per-step path of the reference with host buffers: every step
-           copies the state from pinned host memory, runs the step and copies
-           the new state and the Courant number back (gclaw_step_host).
+           moves the state from pinned host memory to the GPU, runs the step
+           and moves the new state and the Courant number back
+           (gclaw_step_host; pinned arrays are read and written by the step
+           kernel over NVLink-C2C).  e2e_pageable: the same loop on pageable
+           host arrays (numpy), staged through device buffers.
   roofline the dominant kernel (the step) against HBM bandwidth: algorithmic
            bytes 2*m*8 = 48 B per cell-update; an FP64-pipe roofline is given
            beside it because the FP64 step is bound by the FP64 units.
@@ -219,9 +222,10 @@ def run_variant(w, precision, steps, warmup, torch, flush, world, device):
     return secs, accepted, c, dev
 
 
-def e2e_host_steps(w, nsteps, torch, device):
-    """Per-step host-buffer path through gclaw_step_host (pinned buffers),
-    with PyClaw's host-side dt control.  Returns (seconds, accepted, bytes)."""
+def e2e_host_steps(w, nsteps, torch, device, pinned=True):
+    """Per-step host-buffer path through gclaw_step_host (pinned buffers, or
+    pageable numpy arrays), with PyClaw's host-side dt control.  Returns
+    (seconds, accepted, bytes)."""
     from clawpack_gb300 import _lib
 
     s = w.solver_struct(0)
@@ -230,7 +234,7 @@ def e2e_host_steps(w, nsteps, torch, device):
     ws = torch.empty(nb + 256, dtype=torch.uint8, device=device)
     base = (ws.data_ptr() + 255) // 256 * 256
     qb = w.q0.nbytes
-    h = [torch.empty(qb, dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+    h = [torch.empty(qb, dtype=torch.uint8, pin_memory=pinned) for _ in range(2)]
     np.frombuffer(h[0].numpy(), dtype=np.float64)[:] = np.asfortranarray(w.q0).ravel(order="F")
     cfl = ctypes.c_double()
     stream = torch.cuda.current_stream()
@@ -582,8 +586,15 @@ def run_ours(args):
     out["e2e"] = {"value": round(world * cells * e2e_acc / e2e_s * 1e-9, 4), "unit": UNIT,
                   "h2d_bytes_per_step": qb, "d2h_bytes_per_step": qb + 8 + 4,
                   "steps": args.e2e_steps,
-                  "path": "gclaw_step_host: pinned host q -> device, fused BC + step, "
-                          "new q and CFL -> host, every step"}
+                  "path": "gclaw_step_host every step: pinned host q read by the fused BC + "
+                          "step kernel over NVLink-C2C, new q written to pinned host memory, "
+                          "CFL -> host, host dt control"}
+    p_s, p_acc, _ = e2e_host_steps(w, args.e2e_steps, torch, device, pinned=False)
+    p_s = max_over_ranks(p_s, world, device)
+    out["e2e_pageable"] = {"value": round(world * cells * p_acc / p_s * 1e-9, 4), "unit": UNIT,
+                           "path": "gclaw_step_host every step on pageable host arrays: "
+                                   "copies through device buffers, four bands overlapping "
+                                   "the copies"}
     if rank == 0 and world == 1 and not args.no_cpu:
         cw = w
         out["cpu_baseline"] = cpu_baseline(cw)

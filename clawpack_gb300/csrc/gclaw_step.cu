@@ -401,6 +401,22 @@ static int host_bands(const gclaw_solver *s) {
     return nty >= 2 * GCLAW_HOST_BANDS ? GCLAW_HOST_BANDS : 1;
 }
 
+// Device addresses of pinned host arrays (both, or neither).
+static void host_mapped(const double *q_host, double *qnew_host, const double **q_map,
+                        double **new_map) {
+    cudaPointerAttributes ai, ao;
+    if (cudaPointerGetAttributes(&ai, q_host) != cudaSuccess ||
+        cudaPointerGetAttributes(&ao, qnew_host) != cudaSuccess) {
+        cudaGetLastError();  // clear the error state of the lookup
+        return;
+    }
+    if (ai.type == cudaMemoryTypeHost && ao.type == cudaMemoryTypeHost && ai.devicePointer &&
+        ao.devicePointer) {
+        *q_map = (const double *)ai.devicePointer;
+        *new_map = (double *)ao.devicePointer;
+    }
+}
+
 static int step_host_banded(const gclaw_solver *s, const double *q_host, double *qnew_host,
                             double dt, double *d_q, double *d_new, gclaw_ctrl *ws,
                             cudaStream_t st, HostPipe *pp, int nband) {
@@ -734,9 +750,18 @@ int gclaw_step_host(const gclaw_solver *s, const double *q_host, double *qnew_ho
     // the workspace is raw caller memory: clear the control block whose
     // reduction slots and block counter the step expects at zero
     if (cudaMemsetAsync(ws, 0, sizeof(gclaw_ctrl), st) != cudaSuccess) return GCLAW_ERR_CUDA;
+    // Pinned (page-locked) host arrays are addressable from the GPU: the step
+    // then reads q and writes the new state through NVLink-C2C itself, with
+    // no staging copy.  Other host memory goes through the device buffers.
+    const double *q_map = nullptr;
+    double *new_map = nullptr;
+    host_mapped(q_host, qnew_host, &q_map, &new_map);
     HostPipe *pp = nullptr;
     const int nband = host_bands(s);
-    if (nband > 1 && host_pipe(&pp) == GCLAW_OK) {
+    if (q_map && new_map) {
+        rc = gclaw_step(s, q_map, new_map, dt, ws, stream);
+        if (rc) return rc;
+    } else if (nband > 1 && host_pipe(&pp) == GCLAW_OK) {
         rc = step_host_banded(s, q_host, qnew_host, dt, d_q, d_new, ws, st, pp, nband);
         if (rc) return rc;
     } else {

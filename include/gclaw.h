@@ -222,10 +222,13 @@ size_t gclaw_step_workspace_bytes(const gclaw_solver *s);
  * (upstream pyclaw/src/pyclaw/classic/solver.py), here replacing
  * _apply_bcs + step2.  Copies q_host (num_eqn, mx, my) to the device, runs
  * gclaw_step, copies the new state to qnew_host and the Courant number to
- * *cfl_out, then synchronises the stream.  FP64 tile steps of grids of at
- * least eight tile rows without a periodic y boundary run band by band,
- * with the row copies on an internal stream overlapping the bands (same
- * result); host memory should be pinned for the copies to overlap.  ws_dev (caller-owned, 256-byte
+ * *cfl_out, then synchronises the stream.  Pinned host arrays
+ * (cudaHostAlloc / cudaHostRegister, e.g. torch pin_memory) are read and
+ * written by the step kernel itself over NVLink-C2C, without staging
+ * copies; other host memory is copied, and FP64 tile steps of grids of at
+ * least eight tile rows without a periodic y boundary then run band by
+ * band, the row copies on an internal stream overlapping the bands.  The
+ * result is the same bits either way.  ws_dev (caller-owned, 256-byte
  * aligned, at least gclaw_step_workspace_bytes, any contents) holds the
  * control block, which each call clears, and both device states. */
 int gclaw_step_host(const gclaw_solver *s, const double *q_host, double *qnew_host, double dt,

@@ -109,3 +109,39 @@ def test_evolve_host_matches_device_evolve(cuda):
     assert math.isclose(ctrl.t, tend, rel_tol=0, abs_tol=1e-14)
     assert (ctrl.t, ctrl.numsteps, ctrl.attempts) == (c.t, c.numsteps, c.attempts)
     assert np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("rp,prec", [(2, 0), (3, 0), (2, 1)])
+def test_step_host_pinned_arrays_zero_copy(cuda, oracle, rp, prec):
+    """Pinned host arrays: the step reads and writes them directly; the same
+    bits as the oracle (strict build, FP64) or as the pageable path (FP32)."""
+    mx, my = 90, 140
+    rng = np.random.default_rng(31 + rp)
+    q = np.asfortranarray(random_state(rp, mx, my, rng))
+    dx, dy = 1.0 / mx, 1.0 / my
+    dt = 0.05 * min(dx, dy)
+    bcl, bcu = [3, 1], [1, 3]
+    s = make_solver_struct(rp, mx, my, dx, dy, bcl, bcu, [4] * SHAPES[rp][1], 2, 2, prec,
+                           PD[rp])
+    L = _lib.lib(strict=prec == 0)
+    nb = L.gclaw_step_workspace_bytes(ctypes.byref(s))
+    buf, base = aligned_workspace(nb, 0xFF)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    pin_in = torch.from_numpy(np.ascontiguousarray(q.T)).pin_memory()
+    pin_out = torch.empty_like(pin_in).pin_memory()
+    cfl = ctypes.c_double(-1.0)
+    st = L.gclaw_step_host(ctypes.byref(s), ctypes.c_void_p(pin_in.data_ptr()),
+                           ctypes.c_void_p(pin_out.data_ptr()), dt, ctypes.c_void_p(base), nb,
+                           ctypes.byref(cfl), stream)
+    assert st == 0
+    out = np.asfortranarray(pin_out.numpy().T)
+    if prec == 0:
+        qo, cflo, rc = oracle.step(rp, PD[rp], q, dx, dy, dt, bcl, bcu, 2, 2, [4] * 4)
+        assert np.array_equal(out, qo)
+        assert cfl.value == cflo
+    else:
+        ref = np.empty_like(q, order="F")
+        cfl2 = ctypes.c_double(-1.0)
+        assert L.gclaw_step_host(ctypes.byref(s), ptr(q), ptr(ref), dt, ctypes.c_void_p(base),
+                                 nb, ctypes.byref(cfl2), stream) == 0
+        assert np.array_equal(out, ref) and cfl.value == cfl2.value
