@@ -102,6 +102,7 @@ CTRL_BYTES = ctypes.sizeof(GclawCtrl)
 
 # include/gclaw3.h: the unsplit 3D step
 RP3_ACOUSTICS_3D = 1
+RP3_EULER_3D = 2
 
 
 class GclawSolver3(ctypes.Structure):

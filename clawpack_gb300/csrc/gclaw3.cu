@@ -48,7 +48,7 @@ struct Args3 {
 // a is q[1 + a] (upstream riemann rpn3/rpt3/rptt3_acoustics.f90).
 template <typename T>
 struct Rp3Acoustics {
-    static constexpr int M = 4, MW = 2;
+    static constexpr int M = 4, MW = 2, NR = 0;
     struct Params {
         T cc, zz, hz;  // hz = 1 / (2 zz)
     };
@@ -79,8 +79,8 @@ struct Rp3Acoustics {
     }
 
     template <int D>
-    __device__ __forceinline__ static void rpn3(const Params &P, const T *ql, const T *qr, T *W,
-                                                T *s, T *am, T *ap) {
+    __device__ __forceinline__ static bool rpn3(const Params &P, const T *ql, const T *qr, T *W,
+                                                T *s, T *am, T *ap, T *) {
         constexpr int mn = 1 + D;
         const T cc = P.cc, zz = P.zz;
         const T d0 = qr[0] - ql[0];
@@ -98,11 +98,13 @@ struct Rp3Acoustics {
             am[k] = s[0] * W[k];
             ap[k] = s[1] * W[4 + k];
         }
+        return false;
     }
 
     // split asdq along axis t into the parts moving down (bm) and up (bp)
     template <int TA>
-    __device__ __forceinline__ static void rpt3(const Params &P, const T *asdq, T *bm, T *bp) {
+    __device__ __forceinline__ static void rpt3(const Params &P, const T *, const T *asdq, T *bm,
+                                                T *bp) {
         constexpr int mt = 1 + TA;
         const T cc = P.cc, zz = P.zz;
         const T a1 = amp(P, -asdq[0] + zz * asdq[mt]);
@@ -116,8 +118,117 @@ struct Rp3Acoustics {
     // split a fluctuation already split along T1 along T2 (constant
     // coefficients: the split along T2 does not depend on the state)
     template <int T1, int T2>
-    __device__ __forceinline__ static void rptt3(const Params &P, const T *b, T *cm, T *cp) {
-        rpt3<T2>(P, b, cm, cp);
+    __device__ __forceinline__ static void rptt3(const Params &P, const T *R, const T *b, T *cm,
+                                                 T *cp) {
+        rpt3<T2>(P, R, b, cm, cp);
+    }
+};
+
+// 3D Euler, q = (rho, rho u, rho v, rho w, E), Roe solver with three wave
+// families: acoustic (u_d - a), the entropy and both shear waves together
+// (u_d), acoustic (u_d + a); no entropy fix (upstream riemann
+// rpn3/rpt3/rptt3_euler.f90).  The Roe state of the edge, R = (u, v, w, H,
+// a, (gamma-1)/a^2, H - |u|^2, |u|^2), is stored with the edge record and
+// gives the transverse and corner splits their eigenstructure.
+template <typename T>
+struct Rp3Euler {
+    static constexpr int M = 5, MW = 3, NR = 8;
+    struct Params {
+        T gamma1;
+    };
+    static Params make(const double *pd) { return Params{(T)(pd[0] - 1.0)}; }
+
+    template <int D>
+    __host__ __device__ static constexpr bool chain_nz(int, int, int) { return true; }
+
+    __device__ __forceinline__ static T pressure(T gamma1, const T *q) {
+        return gamma1 * (q[4] - qdiv((T)0.5 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]), q[0]));
+    }
+
+    // Roe state; true if the averaged sound speed squared is not positive
+    __device__ __forceinline__ static bool roe(const Params &P, const T *ql, const T *qr, T *R) {
+        const T gamma1 = P.gamma1;
+        const T rl = sqrt(ql[0]), rr = sqrt(qr[0]);
+        const T pl = pressure(gamma1, ql), pr = pressure(gamma1, qr);
+        const T rs = rl + rr;
+#pragma unroll
+        for (int k = 0; k < 3; k++) R[k] = qdiv(qdiv(ql[1 + k], rl) + qdiv(qr[1 + k], rr), rs);
+        R[3] = qdiv(qdiv(ql[4] + pl, rl) + qdiv(qr[4] + pr, rr), rs);
+        R[7] = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+        const T c2 = gamma1 * (R[3] - (T)0.5 * R[7]);
+        R[4] = sqrt(c2);
+        R[5] = qdiv(gamma1, c2);
+        R[6] = R[3] - R[7];
+        return !gt0(c2);
+    }
+
+    // the three waves of vector dq along axis DD and their speeds
+    template <int DD>
+    __device__ __forceinline__ static void waves(const T *R, const T *dq, T *w, T *s) {
+        constexpr int t1 = (DD + 1) % 3, t2 = (DD + 2) % 3;
+        constexpr int mn = 1 + DD, m1 = 1 + t1, m2 = 1 + t2;
+        const T un = R[DD], v1 = R[t1], v2 = R[t2], a = R[4], enth = R[3];
+        const T a2 = R[5] * (R[6] * dq[0] + un * dq[mn] + v1 * dq[m1] + v2 * dq[m2] - dq[4]);
+        const T a3 = dq[m1] - v1 * dq[0];
+        const T a4 = dq[m2] - v2 * dq[0];
+        const T a5 = qdiv(dq[mn] + (a - un) * dq[0] - a * a2, (T)2 * a);
+        const T a1 = dq[0] - a2 - a5;
+        T *w1 = w, *w2 = w + 5, *w3 = w + 10;
+        w1[0] = a1; w1[mn] = a1 * (un - a); w1[m1] = a1 * v1; w1[m2] = a1 * v2;
+        w1[4] = a1 * (enth - un * a);
+        s[0] = un - a;
+        w2[0] = a2; w2[mn] = a2 * un; w2[m1] = a2 * v1 + a3; w2[m2] = a2 * v2 + a4;
+        w2[4] = a2 * (T)0.5 * R[7] + a3 * v1 + a4 * v2;
+        s[1] = un;
+        w3[0] = a5; w3[mn] = a5 * (un + a); w3[m1] = a5 * v1; w3[m2] = a5 * v2;
+        w3[4] = a5 * (enth + un * a);
+        s[2] = un + a;
+    }
+
+    template <int D>
+    __device__ __forceinline__ static bool rpn3(const Params &P, const T *ql, const T *qr, T *W,
+                                                T *s, T *am, T *ap, T *R) {
+        const bool bad = roe(P, ql, qr, R);
+        T dq[5];
+#pragma unroll
+        for (int k = 0; k < 5; k++) dq[k] = qr[k] - ql[k];
+        waves<D>(R, dq, W, s);
+#pragma unroll
+        for (int k = 0; k < 5; k++) am[k] = ap[k] = (T)0;
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+            const bool neg = lt0(s[p]);
+#pragma unroll
+            for (int k = 0; k < 5; k++) {
+                if (neg) am[k] = am[k] + s[p] * W[5 * p + k];
+                else ap[k] = ap[k] + s[p] * W[5 * p + k];
+            }
+        }
+        return bad;
+    }
+
+    template <int TA>
+    __device__ __forceinline__ static void rpt3(const Params &, const T *R, const T *asdq, T *bm,
+                                                T *bp) {
+        T w[15], sb[3];
+        waves<TA>(R, asdq, w, sb);
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            T lo = (T)0, hi = (T)0;
+#pragma unroll
+            for (int p = 0; p < 3; p++) {
+                lo = lo + neg_part(sb[p]) * w[5 * p + k];
+                hi = hi + pos_part(sb[p]) * w[5 * p + k];
+            }
+            bm[k] = lo;
+            bp[k] = hi;
+        }
+    }
+
+    template <int T1, int T2>
+    __device__ __forceinline__ static void rptt3(const Params &P, const T *R, const T *b, T *cm,
+                                                 T *cp) {
+        rpt3<T2>(P, R, b, cm, cp);
     }
 };
 
@@ -154,7 +265,8 @@ template <class RP>
 struct Fields {
     static constexpr int M = RP::M, MW = RP::MW, NCH = chain_slots<RP, 0>();
     static_assert(NCH == chain_slots<RP, 1>() && NCH == chain_slots<RP, 2>(), "slot count");
-    static constexpr int W = 0, S = MW * M, AM = S + MW, AP = AM + M, FA = AP + M;
+    static constexpr int NR = RP::NR > 0 ? RP::NR : 1;
+    static constexpr int W = 0, S = MW * M, AM = S + MW, AP = AM + M, R = AP + M, FA = R + NR;
     static constexpr int AMC = FA + M, APC = AMC + NCH, NF = APC + NCH;
 };
 
@@ -247,8 +359,8 @@ __global__ void __launch_bounds__(NT3) k_edges(const Args3 a, const typename RPT
             ql[k] = from_double<T>(load_q3<M>(a, qin, k, l[0], l[1], l[2]));
             qr[k] = from_double<T>(load_q3<M>(a, qin, k, p[0], p[1], p[2]));
         }
-        T W[MW * M], s[MW], am[M], ap[M];
-        RP::template rpn3<D>(P, ql, qr, W, s, am, ap);
+        T W[MW * M], s[MW], am[M], ap[M], R[F::NR];
+        const bool eb = RP::template rpn3<D>(P, ql, qr, W, s, am, ap, R);
         T *ws = static_cast<T *>(a.ws);
         const long long np = a.npos;
 #pragma unroll
@@ -260,8 +372,12 @@ __global__ void __launch_bounds__(NT3) k_edges(const Args3 a, const typename RPT
             ws[(F::AM + k) * np + idx] = am[k];
             ws[(F::AP + k) * np + idx] = ap[k];
         }
+#pragma unroll
+        for (int r = 0; r < RP::NR; r++) ws[(F::R + r) * np + idx] = R[r];
         // Courant numbers of the edges 0..n along the sweep in every slice
         // (ghost slices included, as the serial sweep counts them)
+        // non-physical states on any edge of the slices the sweep uses
+        if (p[T1] <= a.n[T1] && p[T2] <= a.n[T2]) bad |= eb;
         if (p[D] >= 0 && p[D] <= a.n[D] && p[T1] <= a.n[T1] && p[T2] <= a.n[T2]) {
 #pragma unroll
             for (int q = 0; q < MW; q++) {
@@ -286,13 +402,14 @@ __global__ void __launch_bounds__(NT3) k_edges(const Args3 a, const typename RPT
 
 // ---- k_chains: limiter, correction flux, transverse chains -----------------
 template <class RP, int D, typename T>
-__device__ __forceinline__ void chain(const typename RP::Params &P, const T *asdq, bool dbl, T h,
-                                      T f1, T f2, T *ws, long long np, long long idx, int base) {
+__device__ __forceinline__ void chain(const typename RP::Params &P, const T *R, const T *asdq,
+                                      bool dbl, T h, T f1, T f2, T *ws, long long np,
+                                      long long idx, int base) {
     constexpr int M = RP::M;
     constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
     T bm[M], bp[M], cm[M], cp[M];
-    RP::template rpt3<T1>(P, asdq, bm, bp);
-    RP::template rpt3<T2>(P, asdq, cm, cp);
+    RP::template rpt3<T1>(P, R, asdq, bm, bp);
+    RP::template rpt3<T2>(P, R, asdq, cm, cp);
     T g[2][3][M], hh[2][3][M];
 #pragma unroll
     for (int s = 0; s < 2; s++)
@@ -311,7 +428,7 @@ __device__ __forceinline__ void chain(const typename RP::Params &P, const T *asd
         T cmb[M], cpb[M];
 #pragma unroll
         for (int s = 0; s < 2; s++) {
-            RP::template rptt3<T1, T2>(P, s ? bp : bm, cmb, cpb);
+            RP::template rptt3<T1, T2>(P, R, s ? bp : bm, cmb, cpb);
 #pragma unroll
             for (int k = 0; k < M; k++) {
                 g[s][1][k] = g[s][1][k] + f2 * (cpb[k] - cmb[k]);
@@ -321,7 +438,7 @@ __device__ __forceinline__ void chain(const typename RP::Params &P, const T *asd
         }
 #pragma unroll
         for (int s = 0; s < 2; s++) {
-            RP::template rptt3<T2, T1>(P, s ? cp : cm, cmb, cpb);
+            RP::template rptt3<T2, T1>(P, R, s ? cp : cm, cmb, cpb);
 #pragma unroll
             for (int k = 0; k < M; k++) {
                 hh[s][1][k] = hh[s][1][k] + f1 * (cpb[k] - cmb[k]);
@@ -432,8 +549,11 @@ __global__ void __launch_bounds__(NT3) k_chains(const Args3 a, const typename RP
         const T h = (T)0.5 * dtdn;
         const T sixth = (T)(1.0 / 6.0);
         const T f1 = sixth * dtdn * dtt1, f2 = sixth * dtdn * dtt2;
-        chain<RP, D, T>(P, am, dbl, h, f1, f2, ws, np, idx, F::AMC);
-        chain<RP, D, T>(P, ap, dbl, h, f1, f2, ws, np, idx, F::APC);
+        T R[F::NR];
+#pragma unroll
+        for (int r = 0; r < RP::NR; r++) R[r] = ws[(F::R + r) * np + idx];
+        chain<RP, D, T>(P, R, am, dbl, h, f1, f2, ws, np, idx, F::AMC);
+        chain<RP, D, T>(P, R, ap, dbl, h, f1, f2, ws, np, idx, F::APC);
     } else {
 #pragma unroll
         for (int e = 0; e < F::NCH; e++) {
@@ -598,6 +718,7 @@ extern "C" {
 int gclaw3_rp_shape(int rp, int *num_eqn, int *num_waves) {
     switch (rp) {
     case GCLAW3_RP_ACOUSTICS_3D: *num_eqn = 4; *num_waves = 2; return GCLAW_OK;
+    case GCLAW3_RP_EULER_3D: *num_eqn = 5; *num_waves = 3; return GCLAW_OK;
     default: return GCLAW_ERR_ARG;
     }
 }
@@ -624,14 +745,19 @@ int gclaw3_check(const gclaw3_solver *s) {
     if (tw != 0 && tw != 10 && tw != 11 && tw != 20 && tw != 22) return GCLAW_ERR_UNSUPPORTED;
     if (s->precision != GCLAW_PREC_FP64 && s->precision != GCLAW_PREC_FP32_BULK)
         return GCLAW_ERR_UNSUPPORTED;
-    if (!(s->problem_data[2] > 0.0) || !(s->problem_data[3] > 0.0)) return GCLAW_ERR_ARG;
+    if (s->rp == GCLAW3_RP_ACOUSTICS_3D &&
+        (!(s->problem_data[2] > 0.0) || !(s->problem_data[3] > 0.0)))
+        return GCLAW_ERR_ARG;
+    if (s->rp == GCLAW3_RP_EULER_3D && !(s->problem_data[0] > 1.0)) return GCLAW_ERR_ARG;
     return GCLAW_OK;
 }
 
 size_t gclaw3_workspace_bytes(const gclaw3_solver *s) {
     if (gclaw3_check(s)) return 0;
     const size_t elem = s->precision == GCLAW_PREC_FP64 ? sizeof(double) : sizeof(float);
-    return elem * (size_t)Fields<Rp3Acoustics<double>>::NF * (size_t)box_positions(s);
+    const size_t nf = s->rp == GCLAW3_RP_EULER_3D ? (size_t)Fields<Rp3Euler<double>>::NF
+                                                  : (size_t)Fields<Rp3Acoustics<double>>::NF;
+    return elem * nf * (size_t)box_positions(s);
 }
 
 int gclaw3_step(const gclaw3_solver *s, const double *q_dev, double *qnew_dev, double dt,
@@ -651,7 +777,8 @@ int gclaw3_step(const gclaw3_solver *s, const double *q_dev, double *qnew_dev, d
     a.ws = ws_dev;
     a.dt = dt;
     a.ctrl_mode = 0;
-    return step_all<Rp3Acoustics>(s, a, st, 1);
+    return s->rp == GCLAW3_RP_EULER_3D ? step_all<Rp3Euler>(s, a, st, 1)
+                                       : step_all<Rp3Acoustics>(s, a, st, 1);
 }
 
 int gclaw3_advance(const gclaw3_solver *s, double *q0_dev, double *q1_dev, void *ws_dev,
@@ -670,7 +797,9 @@ int gclaw3_advance(const gclaw3_solver *s, double *q0_dev, double *q1_dev, void 
     a.ws = ws_dev;
     a.dt = 0.0;
     a.ctrl_mode = 1;
-    return step_all<Rp3Acoustics>(s, a, (cudaStream_t)stream, nsteps);
+    cudaStream_t st = (cudaStream_t)stream;
+    return s->rp == GCLAW3_RP_EULER_3D ? step_all<Rp3Euler>(s, a, st, nsteps)
+                                       : step_all<Rp3Acoustics>(s, a, st, nsteps);
 }
 
 }  // extern "C"

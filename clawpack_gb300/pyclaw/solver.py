@@ -396,6 +396,8 @@ class ClawSolver3D(ClawSolver2D):
 
     def _problem_data(self, state):
         pd = state.problem_data
+        if self.rp.rp_id == _lib.RP3_EULER_3D:
+            return [float(pd["gamma"])]
         rho = float(pd["rho"])
         bulk = float(pd["bulk"])
         cc = float(pd["cc"]) if "cc" in pd else math.sqrt(bulk / rho)

@@ -37,6 +37,8 @@ shallow_bathymetry_fwave_2D = _descriptor("shallow_bathymetry_fwave_2D",
 
 # 3D (ClawSolver3D): constant-coefficient acoustics, q = (p, u, v, w)
 acoustics_3D = _descriptor("acoustics_3D", _lib.RP3_ACOUSTICS_3D, num_dim=3)
+# 3D Euler, q = (rho, rho u, rho v, rho w, E), Roe with 3 wave families
+euler_3D = _descriptor("euler_3D", _lib.RP3_EULER_3D, num_dim=3)
 
 __all__ = ["acoustics_2D", "shallow_roe_with_efix_2D", "euler_4wave_2D", "vc_acoustics_2D",
-           "shallow_bathymetry_fwave_2D", "acoustics_3D", "static"]
+           "shallow_bathymetry_fwave_2D", "acoustics_3D", "euler_3D", "static"]

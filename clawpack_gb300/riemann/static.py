@@ -6,6 +6,7 @@ num_eqn = {
     "vc_acoustics_2D": 3,
     "shallow_bathymetry_fwave_2D": 3,
     "acoustics_3D": 4,
+    "euler_3D": 5,
 }
 num_aux = {
     "acoustics_2D": 0,
@@ -14,6 +15,7 @@ num_aux = {
     "vc_acoustics_2D": 2,
     "shallow_bathymetry_fwave_2D": 1,
     "acoustics_3D": 0,
+    "euler_3D": 0,
 }
 num_waves = {
     "acoustics_2D": 2,
@@ -22,4 +24,5 @@ num_waves = {
     "vc_acoustics_2D": 2,
     "shallow_bathymetry_fwave_2D": 3,
     "acoustics_3D": 2,
+    "euler_3D": 3,
 }

@@ -28,6 +28,9 @@ extern "C" {
 
 /* acoustics_3D: m = 4 (p, u, v, w), 2 waves; pd: rho, bulk, cc, zz */
 #define GCLAW3_RP_ACOUSTICS_3D 1
+/* euler_3D: m = 5 (rho, rho u, rho v, rho w, E), 3 waves (acoustic, entropy
+ * and shear together, acoustic), Roe, no entropy fix; pd: gamma */
+#define GCLAW3_RP_EULER_3D 2
 
 typedef struct gclaw3_solver {
     int rp;                       /* GCLAW3_RP_* */

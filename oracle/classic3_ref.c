@@ -10,7 +10,8 @@
  * pyclaw and riemann submodules of the mounted clawpack 5.14.0 tree
  * (.gitmodules:1-21; meson.build:62-76); the upstream files it corresponds
  * to are pyclaw/src/pyclaw/classic/step3.f90, flux3.f90 and
- * riemann/src/rpn3_acoustics.f90, rpt3_acoustics.f90, rptt3_acoustics.f90.
+ * riemann/src/rpn3_acoustics.f90, rpt3_acoustics.f90, rptt3_acoustics.f90 and
+ * rpn3_euler.f90, rpt3_euler.f90, rptt3_euler.f90.
  * This is a restatement, in original code, of the published method the
  * reference cites for it (CITATION.md:46-58): J. O. Langseth and R. J.
  * LeVeque, "A wave propagation method for three-dimensional hyperbolic
@@ -55,6 +56,7 @@
 #endif
 
 #define RP3_ACOUSTICS 1
+#define RP3_EULER 2
 #define RP3_ADVECTION 100 /* constant-velocity advection: a known-answer solver */
 
 #define BC_EXTRAP 1
@@ -75,6 +77,7 @@ static int rp3_shape(int id, int *m, int *mw)
 {
     switch (id) {
     case RP3_ACOUSTICS: *m = 4; *mw = 2; return 0;
+    case RP3_EULER: *m = 5; *mw = 3; return 0;
     case RP3_ADVECTION: *m = 1; *mw = 1; return 0;
     default: return ERR_ARG;
     }
@@ -85,16 +88,87 @@ static int rp3_shape(int id, int *m, int *mw)
  * pd = (rho, bulk, c, Z = rho c); the velocity along axis a is q[1 + a].
  * Advection q = (q) with pd = (u, v, w).
  * ---------------------------------------------------------------------- */
-static void rpn3(const rp3_t *rp, int d, const double *ql, const double *qr, double *wave,
-                 double *s, double *amdq, double *apdq)
+/* 3D Euler, q = (rho, rho u, rho v, rho w, E), pd = (gamma): the Roe state
+ * of an edge (square-root-density averages of the velocity and the total
+ * enthalpy; FVMHP sec. 15.3) and the decomposition of a vector along axis d
+ * into three waves: acoustic (u_d - a), the entropy and the two shear waves
+ * together (u_d), acoustic (u_d + a) (upstream rpn3_euler.f90, which uses
+ * the same three families; no entropy fix). */
+typedef struct {
+    double u[3], enth, a, g1a2, euv, u2;
+    int bad;
+} roe3_t;
+
+static double euler3_pressure(double gamma1, const double *q)
 {
+    return gamma1 * (q[4] - 0.5 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) / q[0]);
+}
+
+static void roe3(const rp3_t *rp, const double *ql, const double *qr, roe3_t *R)
+{
+    const double gamma1 = rp->pd[0] - 1.0;
+    double rhsqrtl = sqrt(ql[0]), rhsqrtr = sqrt(qr[0]);
+    double pl = euler3_pressure(gamma1, ql);
+    double pr = euler3_pressure(gamma1, qr);
+    double rhsq2 = rhsqrtl + rhsqrtr;
+    for (int k = 0; k < 3; k++) R->u[k] = (ql[1 + k] / rhsqrtl + qr[1 + k] / rhsqrtr) / rhsq2;
+    R->enth = ((ql[4] + pl) / rhsqrtl + (qr[4] + pr) / rhsqrtr) / rhsq2;
+    R->u2 = R->u[0] * R->u[0] + R->u[1] * R->u[1] + R->u[2] * R->u[2];
+    double c2 = gamma1 * (R->enth - 0.5 * R->u2);
+    R->bad = !(c2 > 0.0);
+    R->a = sqrt(c2);
+    R->g1a2 = gamma1 / c2;
+    R->euv = R->enth - R->u2;
+}
+
+static void roe3_waves(const roe3_t *R, int d, const double *dq, double *w, double *s)
+{
+    const int t1 = (d + 1) % 3, t2 = (d + 2) % 3;
+    const int mn = 1 + d, m1 = 1 + t1, m2 = 1 + t2;
+    const double un = R->u[d], v1 = R->u[t1], v2 = R->u[t2], a = R->a, enth = R->enth;
+    double a2 = R->g1a2 * (R->euv * dq[0] + un * dq[mn] + v1 * dq[m1] + v2 * dq[m2] - dq[4]);
+    double a3 = dq[m1] - v1 * dq[0];
+    double a4 = dq[m2] - v2 * dq[0];
+    double a5 = (dq[mn] + (a - un) * dq[0] - a * a2) / (2.0 * a);
+    double a1 = dq[0] - a2 - a5;
+    double *w1 = w, *w2 = w + 5, *w3 = w + 10;
+    w1[0] = a1; w1[mn] = a1 * (un - a); w1[m1] = a1 * v1; w1[m2] = a1 * v2;
+    w1[4] = a1 * (enth - un * a);
+    s[0] = un - a;
+    w2[0] = a2; w2[mn] = a2 * un; w2[m1] = a2 * v1 + a3; w2[m2] = a2 * v2 + a4;
+    w2[4] = a2 * 0.5 * R->u2 + a3 * v1 + a4 * v2;
+    s[1] = un;
+    w3[0] = a5; w3[mn] = a5 * (un + a); w3[m1] = a5 * v1; w3[m2] = a5 * v2;
+    w3[4] = a5 * (enth + un * a);
+    s[2] = un + a;
+}
+
+static int rpn3(const rp3_t *rp, int d, const double *ql, const double *qr, double *wave,
+                double *s, double *amdq, double *apdq)
+{
+    if (rp->id == RP3_EULER) {
+        roe3_t R;
+        roe3(rp, ql, qr, &R);
+        double dq[5];
+        for (int k = 0; k < 5; k++) dq[k] = qr[k] - ql[k];
+        roe3_waves(&R, d, dq, wave, s);
+        for (int k = 0; k < 5; k++) amdq[k] = apdq[k] = 0.0;
+        for (int p = 0; p < 3; p++)
+            for (int k = 0; k < 5; k++) {
+                if (s[p] < 0.0)
+                    amdq[k] = amdq[k] + s[p] * wave[5 * p + k];
+                else
+                    apdq[k] = apdq[k] + s[p] * wave[5 * p + k];
+            }
+        return R.bad;
+    }
     if (rp->id == RP3_ADVECTION) {
         const double u = rp->pd[d];
         wave[0] = qr[0] - ql[0];
         s[0] = u;
         amdq[0] = fmin(u, 0.0) * wave[0];
         apdq[0] = fmax(u, 0.0) * wave[0];
-        return;
+        return 0;
     }
     const double cc = rp->pd[2], zz = rp->pd[3];
     const int mn = 1 + d;
@@ -112,11 +186,30 @@ static void rpn3(const rp3_t *rp, int d, const double *ql, const double *qr, dou
         amdq[k] = s[0] * w1[k];
         apdq[k] = s[1] * w2[k];
     }
+    return 0;
 }
 
-/* Split asdq along axis t into the parts moving down (bm) and up (bp). */
-static void rpt3(const rp3_t *rp, int t, const double *asdq, double *bm, double *bp)
+/* Split asdq along axis t into the parts moving down (bm) and up (bp);
+ * ql / qr: the states of the normal edge (Euler: its Roe state). */
+static void rpt3(const rp3_t *rp, int t, const double *ql, const double *qr,
+                 const double *asdq, double *bm, double *bp)
 {
+    if (rp->id == RP3_EULER) {
+        roe3_t R;
+        roe3(rp, ql, qr, &R);
+        double w[15], sb[3];
+        roe3_waves(&R, t, asdq, w, sb);
+        for (int k = 0; k < 5; k++) {
+            double lo = 0.0, hi = 0.0;
+            for (int p = 0; p < 3; p++) {
+                lo = lo + fmin(sb[p], 0.0) * w[5 * p + k];
+                hi = hi + fmax(sb[p], 0.0) * w[5 * p + k];
+            }
+            bm[k] = lo;
+            bp[k] = hi;
+        }
+        return;
+    }
     if (rp->id == RP3_ADVECTION) {
         const double v = rp->pd[t];
         bm[0] = fmin(v, 0.0) * asdq[0];
@@ -133,13 +226,13 @@ static void rpt3(const rp3_t *rp, int t, const double *asdq, double *bm, double 
 }
 
 /* Split a transverse fluctuation (already split along axis t1) along axis
- * t2.  With constant coefficients the eigenstructure along t2 does not
- * depend on the state, so this is rpt3 along t2. */
-static void rptt3(const rp3_t *rp, int t1, int t2, const double *bsasdq, double *cm,
-                  double *cp)
+ * t2, with the eigenstructure of the normal edge's state along t2: rpt3
+ * along t2 (upstream rptt3_*.f90 use the same Roe state). */
+static void rptt3(const rp3_t *rp, int t1, int t2, const double *ql, const double *qr,
+                  const double *bsasdq, double *cm, double *cp)
 {
     (void)t1;
-    rpt3(rp, t2, bsasdq, cm, cp);
+    rpt3(rp, t2, ql, qr, bsasdq, cm, cp);
 }
 
 static double philim3(int id, double r)
@@ -177,13 +270,14 @@ typedef struct {
 /* The chain of one fluctuation asdq: single transverse split and, with
  * double transverse, the corner terms; g[s][o] and h[s][o] are the values
  * it adds to the flux entries of the receiving cell. */
-static void chain(const rp3_t *rp, int t1, int t2, const double *asdq, int dbl, double h,
-                  double f1, double f2, double *g, double *hh)
+static void chain(const rp3_t *rp, int t1, int t2, const double *ql, const double *qr,
+                  const double *asdq, int dbl, double h, double f1, double f2, double *g,
+                  double *hh)
 {
     const int m = rp->m;
     double bm[MAXM], bp[MAXM], cm[MAXM], cp[MAXM];
-    rpt3(rp, t1, asdq, bm, bp);
-    rpt3(rp, t2, asdq, cm, cp);
+    rpt3(rp, t1, ql, qr, asdq, bm, bp);
+    rpt3(rp, t2, ql, qr, asdq, cm, cp);
     for (int e = 0; e < NGH * m; e++) g[e] = hh[e] = 0.0;
 #define GE(s, o, k) g[((s) * 3 + (o)) * m + (k)]
 #define HE(s, o, k) hh[((s) * 3 + (o)) * m + (k)]
@@ -196,7 +290,7 @@ static void chain(const rp3_t *rp, int t1, int t2, const double *asdq, int dbl, 
     if (!dbl) return;
     double cmb[MAXM], cpb[MAXM];
     for (int s = 0; s < 2; s++) {
-        rptt3(rp, t1, t2, s ? bp : bm, cmb, cpb);
+        rptt3(rp, t1, t2, ql, qr, s ? bp : bm, cmb, cpb);
         for (int k = 0; k < m; k++) {
             GE(s, 1, k) = GE(s, 1, k) + f2 * (cpb[k] - cmb[k]);
             GE(s, 2, k) = 0.0 - f2 * cpb[k];
@@ -204,7 +298,7 @@ static void chain(const rp3_t *rp, int t1, int t2, const double *asdq, int dbl, 
         }
     }
     for (int s = 0; s < 2; s++) {
-        rptt3(rp, t2, t1, s ? cp : cm, cmb, cpb);
+        rptt3(rp, t2, t1, ql, qr, s ? cp : cm, cmb, cpb);
         for (int k = 0; k < m; k++) {
             HE(s, 1, k) = HE(s, 1, k) + f1 * (cpb[k] - cmb[k]);
             HE(s, 2, k) = 0.0 - f1 * cpb[k];
@@ -218,7 +312,7 @@ static void chain(const rp3_t *rp, int t1, int t2, const double *asdq, int dbl, 
 /* One slice of n cells along direction d (cells -2..n+1 in q1d). */
 static double flux3_slice(const rp3_t *rp, int d, int n, double dtdn, double dtt1, double dtt2,
                           int order, int tw, const int *mthlim, const work3_t *wk,
-                          const slice_out *out)
+                          const slice_out *out, int *bad)
 {
     const int m = rp->m, mw = rp->mw, off = 2;
     const int t1 = (d + 1) % 3, t2 = (d + 2) % 3;
@@ -234,7 +328,7 @@ static double flux3_slice(const rp3_t *rp, int d, int n, double dtdn, double dtt
 #define FA(c) (out->fadd + (size_t)((c) + off) * m)
 #define GG(c) (out->G + (size_t)((c) + off) * NGH * m)
 #define HH(c) (out->H + (size_t)((c) + off) * NGH * m)
-    for (e = -1; e <= n + 1; e++) rpn3(rp, d, Q(e - 1), Q(e), W(e), S(e), AM(e), AP(e));
+    for (e = -1; e <= n + 1; e++) *bad |= rpn3(rp, d, Q(e - 1), Q(e), W(e), S(e), AM(e), AP(e));
     for (e = -2; e <= n + 1; e++) {
         for (k = 0; k < m; k++) QA(e)[k] = FA(e)[k] = CQ(e)[k] = 0.0;
         for (k = 0; k < NGH * m; k++) GG(e)[k] = HH(e)[k] = 0.0;
@@ -293,14 +387,14 @@ static double flux3_slice(const rp3_t *rp, int d, int n, double dtdn, double dtt
         double g[NGH * MAXM], hh[NGH * MAXM];
         /* A-dQ enters the cell before the edge, A+dQ the cell after it */
         for (e = 0; e <= n; e++) {
-            chain(rp, t1, t2, AM(e), dbl, h, f1, f2, g, hh);
+            chain(rp, t1, t2, Q(e - 1), Q(e), AM(e), dbl, h, f1, f2, g, hh);
             for (k = 0; k < NGH * m; k++) {
                 GG(e - 1)[k] = GG(e - 1)[k] + g[k];
                 HH(e - 1)[k] = HH(e - 1)[k] + hh[k];
             }
         }
         for (e = 0; e <= n; e++) {
-            chain(rp, t1, t2, AP(e), dbl, h, f1, f2, g, hh);
+            chain(rp, t1, t2, Q(e - 1), Q(e), AP(e), dbl, h, f1, f2, g, hh);
             for (k = 0; k < NGH * m; k++) {
                 GG(e)[k] = GG(e)[k] + g[k];
                 HH(e)[k] = HH(e)[k] + hh[k];
@@ -397,7 +491,7 @@ int gclaw3_ref_step3(int rp_id, const double *pd, int mx, int my, int mz, const 
     const int nmax = (mx > my ? (mx > mz ? mx : mz) : (my > mz ? my : mz)) + 4;
     const size_t per = (size_t)nmax * m;
     double cfl = 0.0;
-    int rc = 0;
+    int rc = 0, bad = 0;
 #define QI(arr, k, i, j, l) \
     (arr)[(size_t)(k) + (size_t)m * ((size_t)(i) + (size_t)nb[0] * ((size_t)(j) + (size_t)nb[1] * (size_t)(l)))]
 
@@ -416,7 +510,7 @@ int gclaw3_ref_step3(int rp_id, const double *pd, int mx, int my, int mz, const 
             rc = ERR_ALLOC;
             break;
         }
-#pragma omp parallel num_threads(nthreads)
+#pragma omp parallel num_threads(nthreads) reduction(| : bad)
         {
             work3_t wk;
             wk.q1d = malloc(sizeof(double) * per);
@@ -437,7 +531,7 @@ int gclaw3_ref_step3(int rp_id, const double *pd, int mx, int my, int mz, const 
                 slice_out so = {QA + per * sl, FA + per * sl, GA + per * NGH * sl,
                                 HA + per * NGH * sl};
                 cfls[sl] = flux3_slice(&rp, d, nd, dtd[d], dtd[t1], dtd[t2], order, tw, mthlim,
-                                       &wk, &so);
+                                       &wk, &so, &bad);
             }
             free(wk.q1d); free(wk.wave); free(wk.s); free(wk.amdq); free(wk.apdq); free(wk.cq);
         }
@@ -487,6 +581,7 @@ int gclaw3_ref_step3(int rp_id, const double *pd, int mx, int my, int mz, const 
     }
 #undef QI
     *cfl_out = cfl;
+    if (rc == 0 && bad) rc = 2; /* non-physical state (Euler: c^2 <= 0) */
     return rc;
 }
 
@@ -509,7 +604,7 @@ int gclaw3_ref_step(int rp_id, const double *pd, int mx, int my, int mz, const d
     if (rc == 0)
         rc = gclaw3_ref_step3(rp_id, pd, mx, my, mz, qa, qb, dx, dy, dz, dt, order, tw, mthlim,
                               cfl_out, nthreads);
-    if (rc == 0)
+    if (rc == 0 || rc == 2)
         for (int l = 0; l < mz; l++)
             for (int j = 0; j < my; j++)
                 for (int i = 0; i < mx; i++)
@@ -522,3 +617,14 @@ int gclaw3_ref_step(int rp_id, const double *pd, int mx, int my, int mz, const d
 }
 
 int gclaw3_ref_shape(int rp_id, int *m, int *mw) { return rp3_shape(rp_id, m, mw); }
+
+/* One 3D Riemann problem along axis d (0, 1, 2), for known-answer tests. */
+int gclaw3_ref_rpn3(int rp_id, const double *pd, int d, const double *ql, const double *qr,
+                    double *wave, double *s, double *amdq, double *apdq)
+{
+    rp3_t rp;
+    rp.id = rp_id;
+    if (rp3_shape(rp_id, &rp.m, &rp.mw) || d < 0 || d > 2) return ERR_ARG;
+    memcpy(rp.pd, pd, sizeof rp.pd);
+    return rpn3(&rp, d, ql, qr, wave, s, amdq, apdq) ? 2 : 0;
+}

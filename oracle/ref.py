@@ -282,8 +282,8 @@ def evolve(step_fn, q, t, tend, dt, *, cfl_max=1.0, cfl_desired=0.9, dt_max=1e99
 # 3D (classic3_ref.c): the unsplit 3D step.  q arrays are (m, mx, my, mz).
 # ---------------------------------------------------------------------------
 LIB3 = os.path.join(HERE, "libclassic3_ref.so")
-RP3_ACOUSTICS, RP3_ADVECTION = 1, 100
-SHAPES3 = {RP3_ACOUSTICS: (4, 2), RP3_ADVECTION: (1, 1)}
+RP3_ACOUSTICS, RP3_EULER, RP3_ADVECTION = 1, 2, 100
+SHAPES3 = {RP3_ACOUSTICS: (4, 2), RP3_EULER: (5, 3), RP3_ADVECTION: (1, 1)}
 _lib3 = None
 
 
@@ -299,6 +299,7 @@ def lib3():
         L.gclaw3_ref_fill_ghosts.argtypes = [i, i, i, i, i, ip, ip, dp, dp]
         L.gclaw3_ref_step3.argtypes = [i, dp, i, i, i, dp, dp, d, d, d, d, i, i, ip, dp, i]
         L.gclaw3_ref_step.argtypes = [i, dp, i, i, i, dp, dp, d, d, d, d, i, i, ip, ip, ip, dp, i]
+        L.gclaw3_ref_rpn3.argtypes = [i, dp, i, dp, dp, dp, dp, dp, dp]
         _lib3 = L
     return _lib3
 
@@ -326,9 +327,22 @@ def step3(rp, pd, q, dx, dy, dz, dt, bc_lower, bc_upper, order=2, tw=22, mthlim=
     rc = lib3().gclaw3_ref_step(rp, _dp(_pd(pd)), mx, my, mz, _dp(qf), _dp(qout), dx, dy, dz,
                                 dt, order, tw, _ip(lim), _ip(np.array(bc_lower, np.int32)),
                                 _ip(np.array(bc_upper, np.int32)), _dp(cfl), nthreads)
-    if rc:
+    if rc < 0:
         raise ValueError(f"gclaw3_ref_step failed: {rc}")
+    if rc:
+        raise FloatingPointError(f"gclaw3_ref_step: non-physical state ({rc})")
     return qout, float(cfl[0])
+
+
+def rpn3(rp, pd, d, ql, qr):
+    """One 3D Riemann problem along axis d: (waves (mw, m), s, amdq, apdq, rc)."""
+    m, mw = SHAPES3[rp]
+    ql = np.ascontiguousarray(ql, dtype=np.float64)
+    qr = np.ascontiguousarray(qr, dtype=np.float64)
+    W, s, am, ap = np.zeros(mw * m), np.zeros(mw), np.zeros(m), np.zeros(m)
+    rc = lib3().gclaw3_ref_rpn3(rp, _dp(_pd(pd)), d, _dp(ql), _dp(qr), _dp(W), _dp(s), _dp(am),
+                                _dp(ap))
+    return W.reshape(mw, m), s, am, ap, rc
 
 
 def step3_bc(rp, pd, qbc, dx, dy, dz, dt, order=2, tw=22, mthlim=(4,) * 4, nthreads=1):

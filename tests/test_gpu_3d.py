@@ -168,3 +168,105 @@ def test_fp32_bulk_evolve(cuda, oracle):
         res[prec] = (dev.download(c.parity), c)
     assert res[0][1].numsteps == res[1][1].numsteps
     assert rel_l1(res[1][0], res[0][0]) <= 1e-6
+
+
+# ---------------------------------------------------------------------------
+# euler_3D
+# ---------------------------------------------------------------------------
+def euler3(shape, rng, gamma=1.4):
+    rho = 0.5 + rng.random(shape)
+    u = 0.5 * rng.normal(size=(3,) + shape)
+    p = 0.5 + rng.random(shape)
+    q = np.empty((5,) + shape, order="F")
+    q[0] = rho
+    q[1:4] = rho * u
+    q[4] = p / (gamma - 1.0) + 0.5 * rho * (u ** 2).sum(axis=0)
+    return q
+
+
+def gpu_euler3(q, d, dt, bcl, bcu, order=2, tw=22, lim=4, strict=False, precision=0):
+    m, mx, my, mz = q.shape
+    s = make_solver3_struct(2, mx, my, mz, *d, bcl, bcu, [lim] * 3, order, tw, precision, [1.4])
+    dev = DeviceProblem3(s, strict=strict)
+    dev.upload(q)
+    dev.step(dt, src=0)
+    c = dev.read_ctrl()
+    return dev.download(1), c
+
+
+@pytest.mark.parametrize("shape", [(2, 2, 2), (5, 4, 3), (17, 9, 12)])
+@pytest.mark.parametrize("bcl,bcu", BCS)
+def test_euler_strict_bitwise(cuda, oracle, shape, bcl, bcu):
+    rng = np.random.default_rng(7 * sum(shape) + bcl[0])
+    q = euler3(shape, rng)
+    d = (1.0 / shape[0], 1.1 / shape[1], 0.9 / shape[2])
+    dt = 0.05 * min(d)
+    lim = [1, 2, 3, 4][sum(shape) % 4]
+    qo, cflo = oracle.step3(2, [1.4], q, *d, dt, bcl, bcu, 2, 22, [lim] * 3)
+    qs, c = gpu_euler3(q, d, dt, bcl, bcu, lim=lim, strict=True)
+    assert c.status == 0
+    assert np.array_equal(qs, qo), np.abs(qs - qo).max()
+    assert c.cfl == cflo
+    qp, cp = gpu_euler3(q, d, dt, bcl, bcu, lim=lim)
+    assert rel_l1(qp, qo) <= 1e-13 and abs(cp.cfl - cflo) <= 1e-14 * cflo
+    q32, c32 = gpu_euler3(q, d, dt, bcl, bcu, lim=lim, precision=1)
+    assert rel_l1(q32, qo) <= 2e-6 and abs(c32.cfl - cflo) <= 1e-6 * cflo
+
+
+@pytest.mark.parametrize("order,tw,lim", [(2, 20, 2), (2, 11, 3), (1, 10, 0), (2, 0, 1)])
+def test_euler_options_strict_bitwise(cuda, oracle, order, tw, lim):
+    rng = np.random.default_rng(order * 100 + tw + lim + 1)
+    q = euler3((13, 11, 9), rng)
+    d = (0.1, 0.12, 0.09)
+    dt = 0.004
+    bcl, bcu = [3, 1, 2], [1, 3, 2]
+    qo, cflo = oracle.step3(2, [1.4], q, *d, dt, bcl, bcu, order, tw, [lim] * 3)
+    qs, c = gpu_euler3(q, d, dt, bcl, bcu, order, tw, lim, strict=True)
+    assert np.array_equal(qs, qo)
+    assert c.cfl == cflo
+
+
+def test_euler_nonphysical_state(cuda):
+    rng = np.random.default_rng(3)
+    q = euler3((8, 8, 8), rng)
+    q[4, 3, 4, 5] = 0.01 * q[4, 3, 4, 5] - 5.0  # negative pressure
+    qs, c = gpu_euler3(q, (0.1, 0.1, 0.1), 0.001, [1] * 3, [1] * 3)
+    assert c.status == _lib.NONPHYSICAL
+
+
+def test_euler_clawsolver3d_run(cuda, oracle):
+    """A spherical over-pressure between walls through ClawSolver3D."""
+    from clawpack_gb300 import pyclaw, riemann
+
+    dims = [pyclaw.Dimension(-1.0, 1.0, n, name=c) for n, c in ((18, "x"), (16, "y"), (14, "z"))]
+    domain = pyclaw.Domain(dims)
+    state = pyclaw.State(domain, 5)
+    state.problem_data["gamma"] = 1.4
+    X, Y, Z = state.grid.p_centers
+    p = 1.0 + 2.0 * (X ** 2 + Y ** 2 + Z ** 2 < 0.25)
+    state.q[0] = 1.0
+    state.q[4] = p / 0.4
+    solver = pyclaw.ClawSolver3D(riemann.euler_3D)
+    solver.dimensional_split = False
+    solver.limiters = pyclaw.limiters.tvd.MC
+    solver.bc_lower = [pyclaw.BC.wall] * 3
+    solver.bc_upper = [pyclaw.BC.wall] * 3
+    solver.dt_initial = 0.005
+    claw = pyclaw.Controller()
+    claw.solution = pyclaw.Solution(state, domain)
+    claw.solver = solver
+    claw.tfinal, claw.num_output_times = 0.2, 2
+    q0 = state.q.copy()
+    claw.run()
+    d = tuple(state.grid.delta)
+
+    def step(qq, dt):
+        return oracle.step3(2, [1.4], qq, *d, dt, [3] * 3, [3] * 3, 2, 22, [4] * 3, nthreads=8)
+
+    q, t, dt = q0, 0.0, 0.005
+    for k in range(1, 3):
+        q, t, dt, _ = oracle.evolve(step, q, t, 0.1 * k, dt, cfl_desired=0.9, cfl_max=1.0)
+        assert rel_l1(claw.frames[k].q, q) <= 1e-12, k
+    # mass and energy are conserved between walls
+    for comp in (0, 4):
+        assert abs(claw.frames[-1].q[comp].sum() - q0[comp].sum()) <= 1e-12 * q0[comp].sum()

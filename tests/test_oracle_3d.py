@@ -7,7 +7,11 @@ transverse_waves 0 it is donor cell.  Acoustics on data that do not vary in
 z reproduces the 2D step (the z-transverse and corner terms cancel); the
 step conserves every component with periodic boundaries, keeps a constant
 state bit for bit, commutes with a cyclic permutation of the axes, and
-reports c dt / min(dx, dy, dz) as its Courant number."""
+reports c dt / min(dx, dy, dz) as its Courant number.  The 3D Euler Roe
+solver's waves sum to the jump and their speed-weighted sum to the flux
+difference (the Roe property); at first order, data that do not vary in z
+reproduce the 2D Euler step without entropy fix; it conserves, keeps
+constant states and commutes with the cyclic axis permutation."""
 import math
 
 import numpy as np
@@ -16,7 +20,7 @@ import pytest
 from oracle import ref
 from tests.helpers import rel_l1
 
-AC3, ADV3 = ref.RP3_ACOUSTICS, ref.RP3_ADVECTION
+AC3, EU3, ADV3 = ref.RP3_ACOUSTICS, ref.RP3_EULER, ref.RP3_ADVECTION
 PD3 = [1.0, 4.0, 2.0, 2.0]  # rho, bulk, c, Z
 
 
@@ -119,3 +123,79 @@ def test_unsupported_transverse_option():
     q = random3(4, (4, 4, 4), np.random.default_rng(0))
     with pytest.raises(ValueError):
         ref.step3(AC3, PD3, q, 0.1, 0.1, 0.1, 0.01, [1] * 3, [1] * 3, 2, 21, [4, 4])
+
+
+def euler_state(shape, rng, gamma=1.4):
+    rho = 0.5 + rng.random(shape)
+    u = 0.5 * rng.normal(size=(3,) + shape)
+    p = 0.5 + rng.random(shape)
+    q = np.empty((5,) + shape, order="F")
+    q[0] = rho
+    q[1:4] = rho * u
+    q[4] = p / (gamma - 1.0) + 0.5 * rho * (u ** 2).sum(axis=0)
+    return q
+
+
+def euler_flux(q, d, gamma=1.4):
+    rho, m = q[0], q[1:4]
+    p = (gamma - 1.0) * (q[4] - 0.5 * (m ** 2).sum() / rho)
+    un = m[d] / rho
+    f = un * q
+    f[1 + d] += p
+    f[4] += un * p
+    return f
+
+
+@pytest.mark.parametrize("d", [0, 1, 2])
+@pytest.mark.parametrize("seed", range(3))
+def test_euler_roe_property(d, seed):
+    rng = np.random.default_rng(seed)
+    ql = euler_state((), rng)
+    qr = euler_state((), rng)
+    W, s, am, ap, rc = ref.rpn3(EU3, [1.4], d, ql, qr)
+    assert rc == 0
+    assert np.allclose(W.sum(axis=0), qr - ql, rtol=1e-13, atol=1e-13)
+    df = euler_flux(qr, d) - euler_flux(ql, d)
+    assert np.allclose(am + ap, df, rtol=1e-12, atol=1e-12)
+    assert np.allclose((s[:, None] * W).sum(axis=0), df, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("tw,tw2", [(10, 1), (11, 1), (0, 0)])
+def test_euler_z_uniform_first_order_is_the_2d_step(tw, tw2):
+    rng = np.random.default_rng(40 + tw)
+    mx, my, mz = 13, 11, 4
+    q2 = euler_state((mx, my), rng)
+    q2[3] = 0.0  # no z momentum
+    q2[4] = 1.5 / 0.4 + 0.5 * (q2[1] ** 2 + q2[2] ** 2) / q2[0]
+    q3 = np.zeros((5, mx, my, mz), order="F")
+    q3[0:3] = q2[0:3, ..., None]
+    q3[4] = q2[4, ..., None]
+    dx, dy, dz, dt = 0.1, 0.12, 0.07, 0.005
+    bcl, bcu = [1, 3], [3, 1]
+    out3, cfl3 = ref.step3(EU3, [1.4], q3, dx, dy, dz, dt, bcl + [2], bcu + [2], 1, tw, [0] * 3)
+    q24 = np.asfortranarray(q2[[0, 1, 2, 4]])
+    out2, cfl2, rc = ref.step(3, [1.4, 0.0], q24, dx, dy, dt, bcl, bcu, 1, tw2, [0] * 4)
+    assert rc == 0
+    for l in range(mz):
+        assert rel_l1(out3[[0, 1, 2, 4], :, :, l], out2) <= 1e-14
+    assert np.abs(out3[3]).max() <= 1e-14
+
+
+def test_euler_conservation_constant_state_and_permutation():
+    rng = np.random.default_rng(50)
+    q = euler_state((9, 8, 7), rng)
+    out, _ = ref.step3(EU3, [1.4], q, 0.1, 0.1, 0.1, 0.004, [2] * 3, [2] * 3, 2, 22, [4] * 3)
+    for k in range(5):
+        assert abs(out[k].sum() - q[k].sum()) <= 1e-13 * np.abs(q[k]).sum()
+    c = np.empty((5, 6, 5, 4), order="F")
+    c[:] = euler_state((), rng)[:, None, None, None]
+    outc, _ = ref.step3(EU3, [1.4], c, 0.1, 0.1, 0.1, 0.004, [1, 2, 1], [1, 2, 1], 2, 22,
+                        [4] * 3)
+    assert np.array_equal(outc, c)
+    dx, dy, dz, dt = 0.1, 0.13, 0.08, 0.004
+    a, ca = ref.step3(EU3, [1.4], q, dx, dy, dz, dt, [1, 3, 2], [1, 3, 2], 2, 22, [4] * 3)
+    qp = np.asfortranarray(q.transpose(0, 2, 3, 1)[[0, 2, 3, 1, 4]])
+    b, cb = ref.step3(EU3, [1.4], qp, dy, dz, dx, dt, [3, 2, 1], [3, 2, 1], 2, 22, [4] * 3)
+    back = b[[0, 3, 1, 2, 4]].transpose(0, 3, 1, 2)
+    assert rel_l1(back, a) <= 1e-14
+    assert ca == cb
