@@ -392,6 +392,33 @@ def bench_3d(args, torch, world, device):
         del dev
     a, b = finals["fp32_bulk"], finals["fp64"]
     out["fp32_rel_l1_vs_fp64"] = float((a - b).abs().sum() / b.abs().sum())
+    # 3D Euler (euler_3D, Roe, three wave families) on the seeded octant
+    # problem, 128^3, extrapolation boundaries, superbee-free MC, CFL 0.8
+    ne, esteps = 128, 20
+    eu = {"workload": f"euler_3d_octants {ne}^3 (seed {workloads.EULER3D_SEED}), extrap BCs, "
+                      f"MC, transverse_waves 22, CFL 0.8, {esteps} steps"}
+    for name, prec in (("fp64", 0), ("fp32_bulk", 1)):
+        for prob, k in ((workloads.euler_3d_octants(32), 3),
+                        (workloads.euler_3d_octants(ne), esteps)):
+            dev = DeviceProblem3(prob.solver_struct(precision=prec), device=device)
+            dev.upload(prob.q0)
+            dev.ctrl_init(0.0, prob.dt_initial, math.inf, cfl_max=prob.cfl_max,
+                          cfl_desired=prob.cfl_desired, max_accepted=k, max_steps=10 * k)
+            torch.cuda.synchronize()
+            barrier(world)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dev.advance(k)
+            e1.record()
+            torch.cuda.synchronize()
+            secs = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world, device)
+            c = dev.read_ctrl()
+        eu[name] = {"value": round(world * ne ** 3 * c.numsteps / secs * 1e-9, 4),
+                    "ms_per_step": round(secs / esteps * 1e3, 3),
+                    "accepted_steps": int(c.numsteps), "status": int(c.status)}
+        del dev
+    out["euler_3d"] = eu
+    out["launches"] += 2 * 9 * (esteps + 3)
     if int(os.environ.get("RANK", "0")) == 0:
         from oracle import ref
         small = workloads.acoustics_3d_pulse(48)

@@ -35,7 +35,7 @@ def make_workload(name, mx, my):
 def main(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--workload", default="shallow",
-                   choices=["shallow", "euler", "acoustics", "acoustics3d"])
+                   choices=["shallow", "euler", "acoustics", "acoustics3d", "euler3d"])
     p.add_argument("--mx", type=int, default=2048)
     p.add_argument("--my", type=int, default=None)
     p.add_argument("--steps", type=int, default=20)
@@ -54,7 +54,7 @@ def main(argv=None):
     _lib.lib().gclaw_fp64_kernel({"auto": 0, "tile": 1, "strip": 2}[a.fp64_kernel])
     if a.batched:
         return run_batched(a)
-    if a.workload == "acoustics3d":
+    if a.workload in ("acoustics3d", "euler3d"):
         return run_3d(a)
     w = make_workload(a.workload, a.mx, a.my or a.mx)
     s = w.solver_struct(0 if a.precision == "fp64" else 1)
@@ -84,7 +84,8 @@ def run_3d(a):
     """--warmup then --steps device-controlled 3D steps on an mx^3 cube."""
     from .device import DeviceProblem3
 
-    w = workloads.acoustics_3d_pulse(a.mx)
+    w = (workloads.acoustics_3d_pulse(a.mx) if a.workload == "acoustics3d"
+         else workloads.euler_3d_octants(a.mx))
     dev = DeviceProblem3(w.solver_struct(precision=0 if a.precision == "fp64" else 1))
     dev.upload(w.q0)
     dev.ctrl_init(0.0, w.dt_initial, math.inf, cfl_max=w.cfl_max, cfl_desired=w.cfl_desired,

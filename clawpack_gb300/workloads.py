@@ -337,12 +337,15 @@ class Workload3:
     cfl_desired: float = 0.9
     cfl_max: float = 1.0
 
+    rp_id: int = _lib.RP3_ACOUSTICS_3D
+    num_waves: int = 2
+
     def solver_struct(self, order=2, tw=22, lim=tvd.MC, precision=_lib.PREC_FP64):
         from .device import make_solver3_struct
 
-        return make_solver3_struct(_lib.RP3_ACOUSTICS_3D, self.n, self.n, self.n, *self.delta,
-                                   self.bc_lower, self.bc_upper, [lim, lim], order, tw,
-                                   precision, self.problem_data)
+        return make_solver3_struct(self.rp_id, self.n, self.n, self.n, *self.delta,
+                                   self.bc_lower, self.bc_upper, [lim] * self.num_waves, order,
+                                   tw, precision, self.problem_data)
 
 
 def acoustics_3d_pulse(n=192):
@@ -356,3 +359,28 @@ def acoustics_3d_pulse(n=192):
     # first dt from the sound speed, so no attempt is rejected
     return Workload3("acoustics_3d_pulse", n, (h, h, h), q, [1.0, 4.0, 2.0, 2.0],
                      [BC.wall] * 3, [BC.wall] * 3, dt_initial=0.9 * h / 2.0)
+
+
+EULER3D_SEED = 20261207
+
+
+def euler_3d_octants(n=128, seed=EULER3D_SEED, gamma=1.4):
+    """Eight constant states in the octants of [0, 1]^3 split at the centre
+    (rho, p ~ U[0.5, 1.5], velocity components ~ U[-0.5, 0.5], seeded),
+    extrapolation boundaries: the 3D analogue of the four-quadrant problem."""
+    rng = np.random.default_rng(seed)
+    q = np.zeros((5, n, n, n), order="F")
+    h = n // 2
+    for o in range(8):
+        sl = tuple(slice(0, h) if not (o >> k) & 1 else slice(h, n) for k in range(3))
+        rho = rng.uniform(0.5, 1.5)
+        u = rng.uniform(-0.5, 0.5, size=3)
+        p = rng.uniform(0.5, 1.5)
+        q[(0,) + sl] = rho
+        for k in range(3):
+            q[(1 + k,) + sl] = rho * u[k]
+        q[(4,) + sl] = p / (gamma - 1.0) + 0.5 * rho * float((u ** 2).sum())
+    dx = 1.0 / n
+    return Workload3("euler_3d_octants", n, (dx, dx, dx), q, [gamma], [BC.extrap] * 3,
+                     [BC.extrap] * 3, dt_initial=0.2 * dx, cfl_desired=0.8,
+                     rp_id=_lib.RP3_EULER_3D, num_waves=3)
