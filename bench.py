@@ -393,7 +393,7 @@ def bench_3d(args, torch, world, device):
     a, b = finals["fp32_bulk"], finals["fp64"]
     out["fp32_rel_l1_vs_fp64"] = float((a - b).abs().sum() / b.abs().sum())
     # 3D Euler (euler_3D, Roe, three wave families) on the seeded octant
-    # problem, 128^3, extrapolation boundaries, superbee-free MC, CFL 0.8
+    # problem, 128^3, extrapolation boundaries, MC limiter, CFL 0.8
     ne, esteps = 128, 20
     eu = {"workload": f"euler_3d_octants {ne}^3 (seed {workloads.EULER3D_SEED}), extrap BCs, "
                       f"MC, transverse_waves 22, CFL 0.8, {esteps} steps"}

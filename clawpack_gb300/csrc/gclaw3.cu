@@ -148,7 +148,7 @@ struct Rp3Euler {
     // Roe state; true if the averaged sound speed squared is not positive
     __device__ __forceinline__ static bool roe(const Params &P, const T *ql, const T *qr, T *R) {
         const T gamma1 = P.gamma1;
-        const T rl = sqrt(ql[0]), rr = sqrt(qr[0]);
+        const T rl = tsqrt(ql[0]), rr = tsqrt(qr[0]);
         const T pl = pressure(gamma1, ql), pr = pressure(gamma1, qr);
         const T rs = rl + rr;
 #pragma unroll
@@ -156,7 +156,7 @@ struct Rp3Euler {
         R[3] = qdiv(qdiv(ql[4] + pl, rl) + qdiv(qr[4] + pr, rr), rs);
         R[7] = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
         const T c2 = gamma1 * (R[3] - (T)0.5 * R[7]);
-        R[4] = sqrt(c2);
+        R[4] = tsqrt(c2);
         R[5] = qdiv(gamma1, c2);
         R[6] = R[3] - R[7];
         return !gt0(c2);

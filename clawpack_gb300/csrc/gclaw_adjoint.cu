@@ -181,7 +181,7 @@ __device__ __forceinline__ void adj_sweep(const StepArgs &a, const typename RP::
                 T c = (T)0;
 #pragma unroll
                 for (int p = 0; p < MW; p++) {
-                    const T sa = fabs(s[p]);
+                    const T sa = tabs(s[p]);
                     c = c + sa * ((T)1 - sa * dtave) * (phi[p] * W[p * M + k]);
                 }
                 cq[k] = c;
@@ -220,7 +220,7 @@ __device__ __forceinline__ void adj_sweep(const StepArgs &a, const typename RP::
         if (a.order == 2) {
 #pragma unroll
             for (int p = 0; p < MW; p++) {
-                const T sa = fabs(s[p]);
+                const T sa = tabs(s[p]);
                 const T coef = sa * ((T)1 - sa * dtave);
                 const T dcoef = (s[p] > (T)0 ? (T)1 : (s[p] < (T)0 ? (T)-1 : (T)0)) *
                                 ((T)1 - (T)2 * sa * dtave);

@@ -161,7 +161,7 @@ struct AdjShallow {
             // the intermediate speeds only where the forward's exact pre-test
             // leaves the transonic case open (the same branch decisions)
             if (lt0(s0) && !no_right_sonic_point(h1, hu1, g)) {
-                g1sq = sqrt(g * h1);
+                g1sq = tsqrt(g * h1);
                 s1 = hu1 / h1 - g1sq;
                 trans1 = s1 > (T)0;
             }
@@ -172,7 +172,7 @@ struct AdjShallow {
                 h3 = hr - W[6];
                 hu3 = qr[mu] - W[6 + mu];
                 if (gt0(s03) && !no_right_sonic_point(h3, -hu3, g)) {
-                    g3sq = sqrt(g * h3);
+                    g3sq = tsqrt(g * h3);
                     s3 = hu3 / h3 + g3sq;
                     trans3 = s3 < (T)0;
                 }

@@ -34,10 +34,20 @@
 
 namespace gclaw {
 
+// |a|, sqrt(a), 1/sqrt(a) in the type of a: the float forms by their float
+// names, so that no float operand is widened to a double call.
 template <typename T>
 __device__ __forceinline__ T tabs(T a) { return fabs(a); }
 template <>
 __device__ __forceinline__ float tabs<float>(float a) { return fabsf(a); }
+template <typename T>
+__device__ __forceinline__ T tsqrt(T a) { return sqrt(a); }
+template <>
+__device__ __forceinline__ float tsqrt<float>(float a) { return sqrtf(a); }
+template <typename T>
+__device__ __forceinline__ T trsqrt(T a) { return rsqrt(a); }
+template <>
+__device__ __forceinline__ float trsqrt<float>(float a) { return rsqrtf(a); }
 template <typename T>
 __device__ __forceinline__ T tmin(T a, T b) { return fmin(a, b); }
 template <typename T>
@@ -123,7 +133,7 @@ __device__ __forceinline__ T pos_part(T x) { return gt0(x) ? x : (T)0; }
 
 // Running max of |s| over non-NaN speeds, as fmax(m, fabs(s)) gives it.
 template <typename T>
-__device__ __forceinline__ T max_abs(T m, T s) { return tmax(m, (T)fabs(s)); }
+__device__ __forceinline__ T max_abs(T m, T s) { return tmax(m, tabs(s)); }
 template <>
 __device__ __forceinline__ double max_abs<double>(double m, double s) {
     const long long a = __double_as_longlong(s) & F64_ABS_MASK;
@@ -368,14 +378,14 @@ struct RpShallow {
     // one reciprocal per cell (hu / sqrt h = (hu / h) sqrt h, sqrt(g h) =
     // sqrt(g) sqrt h), within two roundings of the quotients.
     __device__ __forceinline__ static void cell_aux(const Params &P, const T *q, T *aux) {
-        const T hs = sqrt(q[0]);
+        const T hs = tsqrt(q[0]);
         aux[0] = hs;
 #ifdef GCLAW_STRICT
         aux[1] = q[1] / hs;
         aux[2] = q[2] / hs;
         aux[3] = q[1] / q[0];
         aux[4] = q[2] / q[0];
-        aux[5] = sqrt(P.g * q[0]);
+        aux[5] = tsqrt(P.g * q[0]);
 #else
         const T rh = rcp_fast(q[0]);
         aux[3] = q[1] * rh;
@@ -406,14 +416,14 @@ struct RpShallow {
 #ifdef GCLAW_STRICT
             u = (al[mu] + ar[mu]) / hsq2;
             v = (al[mv] + ar[mv]) / hsq2;
-            c = sqrt(P.g * hbar);
+            c = tsqrt(P.g * hbar);
 #else
             // one reciprocal for both averages; c and 0.5 / c from one rsqrt
             const T ri = rcp_fast(hsq2);
             u = (al[mu] + ar[mu]) * ri;
             v = (al[mv] + ar[mv]) * ri;
             const T gh = P.g * hbar;
-            const T rs = rsqrt(gh);
+            const T rs = trsqrt(gh);
             R[0] = u; R[1] = v; R[2] = gh * rs; R[3] = (T)0.5 * rs;
             return;
 #endif
@@ -453,7 +463,7 @@ struct RpShallow {
             T s1 = (T)0, sfract;
             bool sonic1 = false;  // s0 < 0 < s1: transonic 1-rarefaction
             if (lt0(s0) && !no_right_sonic_point(h1, hu1, g)) {
-                s1 = hu1 / h1 - sqrt(g * h1);
+                s1 = hu1 / h1 - tsqrt(g * h1);
                 sonic1 = s1 > (T)0;
             }
             if (sonic1)
@@ -473,7 +483,7 @@ struct RpShallow {
                 T s3 = (T)0;
                 bool sonic3 = false;  // s3 < 0 < s03: transonic 3-rarefaction
                 if (gt0(s03) && !no_right_sonic_point(h3, -hu3, g)) {
-                    s3 = hu3 / h3 + sqrt(g * h3);
+                    s3 = hu3 / h3 + tsqrt(g * h3);
                     sonic3 = s3 < (T)0;
                 }
                 bool add = true;
@@ -664,7 +674,7 @@ struct RpEuler {
     // aux = (sqrt rho, p, rho u / sqrt rho, rho v / sqrt rho, (E + p) / sqrt rho,
     //        u, v, c)
     __device__ __forceinline__ static void cell_aux(const Params &P, const T *q, T *aux) {
-        const T rs = sqrt(q[0]);
+        const T rs = tsqrt(q[0]);
         const T p = pressure(P.gamma1, q);
         aux[0] = rs;
         aux[1] = p;
@@ -673,7 +683,7 @@ struct RpEuler {
         aux[4] = qdiv(q[3] + p, rs);
         aux[5] = qdiv(q[1], q[0]);
         aux[6] = qdiv(q[2], q[0]);
-        aux[7] = sqrt(qdiv(P.gamma * p, q[0]));
+        aux[7] = tsqrt(qdiv(P.gamma * p, q[0]));
     }
 
     template <int IXY>
@@ -700,7 +710,7 @@ struct RpEuler {
         T u2v2 = u * u + v * v;
         T c2 = gamma1 * (enth - (T)0.5 * u2v2);
         bool bad = !(c2 > (T)0);
-        T a = sqrt(c2);
+        T a = tsqrt(c2);
         T g1a2 = qdiv(gamma1, c2);
         T euv = enth - u2v2;
         R[0] = u; R[1] = v; R[2] = enth; R[3] = u2v2; R[4] = a; R[5] = g1a2; R[6] = euv;
@@ -747,7 +757,7 @@ struct RpEuler {
             T rhov1 = ql[mv] + w1[mv];
             T en1 = ql[3] + w1[3];
             T p1 = gamma1 * (en1 - qdiv((T)0.5 * (rhou1 * rhou1 + rhov1 * rhov1), rho1));
-            T c1 = sqrt(qdiv(gamma * p1, rho1));
+            T c1 = tsqrt(qdiv(gamma * p1, rho1));
             T s1 = qdiv(rhou1, rho1) - c1;
             T sfract;
             if (s0 < (T)0 && s1 > (T)0)
@@ -769,7 +779,7 @@ struct RpEuler {
                 T rhov2 = qr[mv] - w4[mv];
                 T en2 = qr[3] - w4[3];
                 T p2 = gamma1 * (en2 - qdiv((T)0.5 * (rhou2 * rhou2 + rhov2 * rhov2), rho2));
-                T cc2 = sqrt(qdiv(gamma * p2, rho2));
+                T cc2 = tsqrt(qdiv(gamma * p2, rho2));
                 T s2 = qdiv(rhou2, rho2) + cc2;
                 bool add = true;
                 if (s2 < (T)0 && s3 > (T)0)
@@ -842,7 +852,7 @@ __device__ __forceinline__ T philim(int id, T r) {
     switch (id) {
     case 1: return tmax((T)0, tmin((T)1, r));
     case 2: return tmax((T)0, tmax(tmin((T)1, (T)2 * r), tmin((T)2, r)));
-    case 3: return (r + fabs(r)) / ((T)1 + fabs(r));
+    case 3: return (r + tabs(r)) / ((T)1 + tabs(r));
     case 4: {
         T c = ((T)1 + r) / (T)2;
         return tmax((T)0, tmin(c, tmin((T)2, (T)2 * r)));

@@ -552,7 +552,7 @@ __device__ __forceinline__ void phase_limit(const typename RP::Params &P, const 
 #pragma unroll
                 for (int p = 0; p < MW; p++) {
                     if (!RP::template wnz<IXY>(p, k)) continue;
-                    const T sa = fabs(s[p]);
+                    const T sa = tabs(s[p]);
                     if constexpr (RP::FWAVE)  // sign(s) (1 - |s| dt/dx) Z
                         c = c + sign_times((T)1 - sa * dtave, s[p]) * W[p * M + k];
                     else
