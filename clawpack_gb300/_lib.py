@@ -161,6 +161,8 @@ SIGNATURES = {
     "gclaw3_workspace_bytes": (_SZ, [_SP3]),
     "gclaw3_step": (_I, [_SP3, _P, _P, _D, _P, _P, _P]),
     "gclaw3_advance": (_I, [_SP3, _P, _P, _P, _P, _I, _P]),
+    "gclaw3_step_split": (_I, [_SP3, _P, _P, _P, _D, _P, _P, _P]),
+    "gclaw3_advance_split": (_I, [_SP3, _P, _P, _P, _P, _P, _I, _P]),
 }
 
 _libs = {}

@@ -35,6 +35,8 @@ constexpr int NT3 = 256;
 struct Args3 {
     const double *qin[2];
     double *qout[2];
+    double *qtmp;  // dimensionally split steps: the state between the y- and z-sweeps
+    int split;     // 1: each sweep starts from the previous one's result
     gclaw_ctrl *ctrl;
     void *ws;  // edge records, in the arithmetic type of the step
     double dt, d[3];
@@ -307,6 +309,17 @@ __device__ __forceinline__ double load_q3(const Args3 &a, const double *__restri
                                 (neg ? (long long)0x8000000000000000ull : 0ll));
 }
 
+// The state a sweep starts from and the one it writes.  Unsplit: every
+// sweep reads the old state, the x-sweep writes the new one and the others
+// add to it.  Split (x, y, z in turn): old -> new -> tmp -> new.
+__device__ __forceinline__ const double *sweep_in(const Args3 &a, int d, int par) {
+    if (!a.split || d == 0) return a.qin[par];
+    return d == 1 ? a.qout[par] : a.qtmp;
+}
+__device__ __forceinline__ double *sweep_out(const Args3 &a, int d, int par) {
+    return a.split && d == 1 ? a.qtmp : a.qout[par];
+}
+
 // dt, parity and skip flag of this launch (device time-step control).
 struct Launch {
     double dt;
@@ -340,7 +353,7 @@ __global__ void __launch_bounds__(NT3) k_edges(const Args3 a, const typename RPT
     constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
     const Launch L = launch_state(a);
     if (L.skip) return;
-    const double *__restrict__ qin = a.qin[L.par];
+    const double *__restrict__ qin = sweep_in(a, D, L.par);
     const T dtdn = (T)(L.dt / a.d[D]);
     T cmax = (T)0;
     bool bad = false;
@@ -583,9 +596,10 @@ __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
         p[0] = (int)(cid % a.n[0]);
         p[1] = (int)((cid / a.n[0]) % a.n[1]);
         p[2] = (int)(cid / ((long long)a.n[0] * a.n[1]));
-        // the x-sweep starts from the old state, the others add to the new one
-        const double *src = D == 0 ? a.qin[L.par] : a.qout[L.par];
-        double *dst = a.qout[L.par];
+        // the x-sweep starts from the old state, the others add to the new
+        // one (unsplit) or start from the previous sweep's result (split)
+        const double *src = a.split ? sweep_in(a, D, L.par) : D == 0 ? a.qin[L.par] : a.qout[L.par];
+        double *dst = sweep_out(a, D, L.par);
         const size_t o = (size_t)M * (size_t)cid;
         const T *ws = static_cast<const T *>(a.ws);
         const long long np = a.npos;
@@ -779,6 +793,58 @@ int gclaw3_step(const gclaw3_solver *s, const double *q_dev, double *qnew_dev, d
     a.ctrl_mode = 0;
     return s->rp == GCLAW3_RP_EULER_3D ? step_all<Rp3Euler>(s, a, st, 1)
                                        : step_all<Rp3Acoustics>(s, a, st, 1);
+}
+
+int gclaw3_step_split(const gclaw3_solver *s, const double *q_dev, double *qnew_dev,
+                      double *qtmp_dev, double dt, void *ws_dev, gclaw_ctrl *ctrl_dev,
+                      void *stream) {
+    int rc = gclaw3_check(s);
+    if (rc) return rc;
+    if (!q_dev || !qnew_dev || !qtmp_dev || !ws_dev || !ctrl_dev || !(dt > 0.0) ||
+        q_dev == qnew_dev || qtmp_dev == q_dev || qtmp_dev == qnew_dev)
+        return GCLAW_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(ctrl_dev, 0, sizeof(gclaw_ctrl), st) != cudaSuccess)
+        return GCLAW_ERR_CUDA;
+    Args3 a{};
+    fill_args(s, a);
+    a.qin[0] = a.qin[1] = q_dev;
+    a.qout[0] = a.qout[1] = qnew_dev;
+    a.qtmp = qtmp_dev;
+    a.split = 1;
+    a.tw = 0;  // split sweeps carry no transverse terms
+    a.ctrl = ctrl_dev;
+    a.ws = ws_dev;
+    a.dt = dt;
+    a.ctrl_mode = 0;
+    return s->rp == GCLAW3_RP_EULER_3D ? step_all<Rp3Euler>(s, a, st, 1)
+                                       : step_all<Rp3Acoustics>(s, a, st, 1);
+}
+
+int gclaw3_advance_split(const gclaw3_solver *s, double *q0_dev, double *q1_dev,
+                         double *qtmp_dev, void *ws_dev, gclaw_ctrl *ctrl_dev, int nsteps,
+                         void *stream) {
+    int rc = gclaw3_check(s);
+    if (rc) return rc;
+    if (!q0_dev || !q1_dev || !qtmp_dev || !ws_dev || !ctrl_dev || nsteps < 0 ||
+        q0_dev == q1_dev || qtmp_dev == q0_dev || qtmp_dev == q1_dev)
+        return GCLAW_ERR_ARG;
+    Args3 a{};
+    fill_args(s, a);
+    a.qin[0] = q0_dev;
+    a.qin[1] = q1_dev;
+    a.qout[0] = q1_dev;
+    a.qout[1] = q0_dev;
+    a.qtmp = qtmp_dev;
+    a.split = 1;
+    a.tw = 0;
+    a.ctrl = ctrl_dev;
+    a.ws = ws_dev;
+    a.dt = 0.0;
+    a.ctrl_mode = 1;
+    cudaStream_t st = (cudaStream_t)stream;
+    return s->rp == GCLAW3_RP_EULER_3D ? step_all<Rp3Euler>(s, a, st, nsteps)
+                                       : step_all<Rp3Acoustics>(s, a, st, nsteps);
 }
 
 int gclaw3_advance(const gclaw3_solver *s, double *q0_dev, double *q1_dev, void *ws_dev,

@@ -184,11 +184,11 @@ class DeviceProblem3(DeviceProblem):
     workspace and a control block on one CUDA device (gclaw3_step /
     gclaw3_advance); time-step control as in 2D."""
 
-    def __init__(self, solver_struct, device=None, strict=False):
+    def __init__(self, solver_struct, device=None, strict=False, split=False):
         self.s = solver_struct
         self.L = L = _lib.lib(strict)
         self.device = torch.device(device or "cuda")
-        self.split = False
+        self.split = bool(split)
         self.aux = None
         _lib.check(L.gclaw3_check(ctypes.byref(self.s)), "gclaw3_check")
         m, mw = ctypes.c_int(), ctypes.c_int()
@@ -198,6 +198,8 @@ class DeviceProblem3(DeviceProblem):
         shape = (self.mz, self.my, self.mx, self.m)
         self.q = [torch.empty(shape, dtype=torch.float64, device=self.device),
                   torch.empty(shape, dtype=torch.float64, device=self.device)]
+        self.qtmp = (torch.empty(shape, dtype=torch.float64, device=self.device)
+                     if self.split else None)
         nbytes = L.gclaw3_workspace_bytes(ctypes.byref(self.s))
         self.ws = torch.empty(int(nbytes), dtype=torch.uint8, device=self.device)
         self.ctrl = torch.zeros(256, dtype=torch.uint8, device=self.device)
@@ -216,6 +218,13 @@ class DeviceProblem3(DeviceProblem):
         return np.asfortranarray(self.q[buf].cpu().numpy().T)
 
     def advance(self, nlaunch, stream=None):
+        if self.split:
+            _lib.check(self.L.gclaw3_advance_split(
+                ctypes.byref(self.s), ctypes.c_void_p(self.q[0].data_ptr()),
+                ctypes.c_void_p(self.q[1].data_ptr()), ctypes.c_void_p(self.qtmp.data_ptr()),
+                ctypes.c_void_p(self.ws.data_ptr()), ctypes.c_void_p(self.ctrl.data_ptr()),
+                int(nlaunch), _stream_handle(stream)), "gclaw3_advance_split")
+            return
         _lib.check(self.L.gclaw3_advance(
             ctypes.byref(self.s), ctypes.c_void_p(self.q[0].data_ptr()),
             ctypes.c_void_p(self.q[1].data_ptr()), ctypes.c_void_p(self.ws.data_ptr()),
@@ -223,6 +232,14 @@ class DeviceProblem3(DeviceProblem):
             "gclaw3_advance")
 
     def step(self, dt, src=0, stream=None):
+        if self.split:
+            _lib.check(self.L.gclaw3_step_split(
+                ctypes.byref(self.s), ctypes.c_void_p(self.q[src].data_ptr()),
+                ctypes.c_void_p(self.q[1 - src].data_ptr()),
+                ctypes.c_void_p(self.qtmp.data_ptr()), float(dt),
+                ctypes.c_void_p(self.ws.data_ptr()), ctypes.c_void_p(self.ctrl.data_ptr()),
+                _stream_handle(stream)), "gclaw3_step_split")
+            return
         _lib.check(self.L.gclaw3_step(
             ctypes.byref(self.s), ctypes.c_void_p(self.q[src].data_ptr()),
             ctypes.c_void_p(self.q[1 - src].data_ptr()), float(dt),

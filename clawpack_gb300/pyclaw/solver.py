@@ -378,8 +378,9 @@ class ClawSolver3D(ClawSolver2D):
     ``transverse_waves`` takes ClawSolver3D's values: 0, 10 / 11
     (``trans_inc``: transverse propagation of the increment waves, without /
     with the corner terms) and 20 / 22 (``trans_cor``: also of the correction
-    waves).  Steps are unsplit (``dimensional_split = False``), without aux
-    arrays, in FP64 or FP32-bulk (``precision``)."""
+    waves).  ``dimensional_split = True`` (the default) takes x-, y- and
+    z-sweeps in turn without transverse terms; ``False`` the unsplit step.
+    Without aux arrays, in FP64 or FP32-bulk (``precision``)."""
     no_trans = 0
     trans_inc = 11
     trans_cor = 22
@@ -415,9 +416,6 @@ class ClawSolver3D(ClawSolver2D):
                 "backend only")
         if self.fwave:
             raise ValueError(f"{self.rp.name} needs solver.fwave = False")
-        if self.dimensional_split:
-            raise NotImplementedError("3D steps are unsplit here; set "
-                                      "solver.dimensional_split = False")
         if state.num_aux or getattr(state, "index_capa", -1) >= 0:
             raise NotImplementedError("3D steps with aux arrays are not supported")
         if self.num_ghost != 2:
@@ -448,8 +446,9 @@ class ClawSolver3D(ClawSolver2D):
 
     def _device(self, state):
         s = self.solver_struct(state)
-        key = (bytes(s), False)
+        split = bool(self.dimensional_split)
+        key = (bytes(s), split)
         if self._dev is None or self._dev_key != key:
-            self._dev = DeviceProblem3(s)
+            self._dev = DeviceProblem3(s, split=split)
             self._dev_key = key
         return self._dev

@@ -68,6 +68,19 @@ int gclaw3_step(const gclaw3_solver *s, const double *q_dev, double *qnew_dev, d
 int gclaw3_advance(const gclaw3_solver *s, double *q0_dev, double *q1_dev, void *ws_dev,
                    gclaw_ctrl *ctrl_dev, int nsteps, void *stream);
 
+/* PyClaw's dimensionally split 3D step (ClawSolver3D with
+ * dimensional_split = True, its default; classic3 step3ds): the x-, y- and
+ * z-sweeps in turn, each from the previous one's result with the boundary
+ * conditions applied to it, without transverse terms (transverse_waves is
+ * ignored); qtmp_dev is a third state buffer, distinct from the others.
+ * The Courant number is the largest of the three sweeps'. */
+int gclaw3_step_split(const gclaw3_solver *s, const double *q_dev, double *qnew_dev,
+                      double *qtmp_dev, double dt, void *ws_dev, gclaw_ctrl *ctrl_dev,
+                      void *stream);
+int gclaw3_advance_split(const gclaw3_solver *s, double *q0_dev, double *q1_dev,
+                         double *qtmp_dev, void *ws_dev, gclaw_ctrl *ctrl_dev, int nsteps,
+                         void *stream);
+
 #ifdef __cplusplus
 }
 #endif

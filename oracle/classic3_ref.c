@@ -472,9 +472,35 @@ int gclaw3_ref_fill_ghosts(int m, int mx, int my, int mz, int g, const int *bc_l
 
 /* The unsplit 3D step on ghost-filled arrays (m, mx+4, my+4, mz+4); qnew
  * receives qold plus all updates. */
+static int step3_dirs(int rp_id, const double *pd, int mx, int my, int mz, const double *qold,
+                      double *qnew, double dx, double dy, double dz, double dt, int order,
+                      int tw, const int *mthlim, double *cfl_out, int nthreads, int d_lo,
+                      int d_hi);
+
 int gclaw3_ref_step3(int rp_id, const double *pd, int mx, int my, int mz, const double *qold,
                      double *qnew, double dx, double dy, double dz, double dt, int order, int tw,
                      const int *mthlim, double *cfl_out, int nthreads)
+{
+    return step3_dirs(rp_id, pd, mx, my, mz, qold, qnew, dx, dy, dz, dt, order, tw, mthlim,
+                      cfl_out, nthreads, 0, 2);
+}
+
+/* The sweep of one direction d (0, 1, 2) alone, without transverse terms:
+ * one stage of PyClaw's dimensionally split 3D step (classic3 step3ds,
+ * upstream pyclaw/src/pyclaw/classic/step3ds.f90), on ghost-filled arrays. */
+int gclaw3_ref_step3ds(int rp_id, const double *pd, int mx, int my, int mz, const double *qold,
+                       double *qnew, double dx, double dy, double dz, double dt, int order,
+                       const int *mthlim, int d, double *cfl_out, int nthreads)
+{
+    if (d < 0 || d > 2) return ERR_ARG;
+    return step3_dirs(rp_id, pd, mx, my, mz, qold, qnew, dx, dy, dz, dt, order, 0, mthlim,
+                      cfl_out, nthreads, d, d);
+}
+
+static int step3_dirs(int rp_id, const double *pd, int mx, int my, int mz, const double *qold,
+                      double *qnew, double dx, double dy, double dz, double dt, int order,
+                      int tw, const int *mthlim, double *cfl_out, int nthreads, int d_lo,
+                      int d_hi)
 {
     rp3_t rp;
     rp.id = rp_id;
@@ -495,7 +521,7 @@ int gclaw3_ref_step3(int rp_id, const double *pd, int mx, int my, int mz, const 
 #define QI(arr, k, i, j, l) \
     (arr)[(size_t)(k) + (size_t)m * ((size_t)(i) + (size_t)nb[0] * ((size_t)(j) + (size_t)nb[1] * (size_t)(l)))]
 
-    for (int d = 0; d < 3 && rc == 0; d++) {
+    for (int d = d_lo; d <= d_hi && rc == 0; d++) {
         const int t1 = (d + 1) % 3, t2 = (d + 2) % 3;
         const int nd = n[d], n1 = n[t1], n2 = n[t2];
         const int ns1 = n1 + 2, ns2 = n2 + 2; /* slices a = -1..n1, b = -1..n2 */
@@ -627,4 +653,51 @@ int gclaw3_ref_rpn3(int rp_id, const double *pd, int d, const double *ql, const 
     if (rp3_shape(rp_id, &rp.m, &rp.mw) || d < 0 || d > 2) return ERR_ARG;
     memcpy(rp.pd, pd, sizeof rp.pd);
     return rpn3(&rp, d, ql, qr, wave, s, amdq, apdq) ? 2 : 0;
+}
+
+/* PyClaw's dimensionally split 3D step (Godunov splitting, ClawSolver3D's
+ * default dimensional_split = True): boundary conditions and the x-sweep,
+ * boundary conditions again on its result and the y-sweep, then the
+ * z-sweep; *cfl_out is the largest of the three sweeps' Courant numbers.
+ * Interior-shaped arrays (m, mx, my, mz). */
+int gclaw3_ref_step_split(int rp_id, const double *pd, int mx, int my, int mz, const double *q,
+                          double *qout, double dx, double dy, double dz, double dt, int order,
+                          const int *mthlim, const int *bc_lower, const int *bc_upper,
+                          double *cfl_out, int nthreads)
+{
+    int m, mw;
+    if (rp3_shape(rp_id, &m, &mw)) return ERR_ARG;
+    const int nx = mx + 4, ny = my + 4, nz = mz + 4;
+    const size_t nb = (size_t)m * nx * ny * nz, ni = (size_t)m * mx * my * mz;
+    double *qa = malloc(sizeof(double) * nb), *qb = malloc(sizeof(double) * nb);
+    double *qi = malloc(sizeof(double) * ni);
+    if (!qa || !qb || !qi) {
+        free(qa); free(qb); free(qi);
+        return ERR_ALLOC;
+    }
+    memcpy(qi, q, sizeof(double) * ni);
+    double cfl = 0.0;
+    int rc = 0, bad = 0;
+    for (int d = 0; d < 3; d++) {
+        double c = 0.0;
+        rc = gclaw3_ref_fill_ghosts(m, mx, my, mz, 2, bc_lower, bc_upper, qi, qa);
+        if (rc) break;
+        rc = gclaw3_ref_step3ds(rp_id, pd, mx, my, mz, qa, qb, dx, dy, dz, dt, order, mthlim, d,
+                                &c, nthreads);
+        if (rc == 2) bad = 1;
+        else if (rc) break;
+        rc = 0;
+        cfl = cfl > c ? cfl : c;
+        for (int l = 0; l < mz; l++)
+            for (int j = 0; j < my; j++)
+                for (int i = 0; i < mx; i++)
+                    for (int k = 0; k < m; k++)
+                        qi[(size_t)k + (size_t)m * ((size_t)i + (size_t)mx * ((size_t)j + (size_t)my * l))] =
+                            qb[(size_t)k + (size_t)m * ((size_t)(i + 2) + (size_t)nx * ((size_t)(j + 2) + (size_t)ny * (l + 2)))];
+    }
+    if (rc == 0) memcpy(qout, qi, sizeof(double) * ni);
+    free(qa); free(qb); free(qi);
+    *cfl_out = cfl;
+    if (rc) return rc;
+    return bad ? 2 : 0;
 }

@@ -300,6 +300,8 @@ def lib3():
         L.gclaw3_ref_step3.argtypes = [i, dp, i, i, i, dp, dp, d, d, d, d, i, i, ip, dp, i]
         L.gclaw3_ref_step.argtypes = [i, dp, i, i, i, dp, dp, d, d, d, d, i, i, ip, ip, ip, dp, i]
         L.gclaw3_ref_rpn3.argtypes = [i, dp, i, dp, dp, dp, dp, dp, dp]
+        L.gclaw3_ref_step_split.argtypes = [i, dp, i, i, i, dp, dp, d, d, d, d, i, ip, ip, ip,
+                                            dp, i]
         _lib3 = L
     return _lib3
 
@@ -358,4 +360,24 @@ def step3_bc(rp, pd, qbc, dx, dy, dz, dt, order=2, tw=22, mthlim=(4,) * 4, nthre
                                  dt, order, tw, _ip(lim), _dp(cfl), nthreads)
     if rc:
         raise ValueError(f"gclaw3_ref_step3 failed: {rc}")
+    return qout, float(cfl[0])
+
+
+def step3_split(rp, pd, q, dx, dy, dz, dt, bc_lower, bc_upper, order=2, mthlim=(4,) * 4,
+                nthreads=1):
+    """PyClaw's dimensionally split 3D step (x, y, z sweeps, boundary
+    conditions before each); returns (qnew, cfl)."""
+    m, mx, my, mz = q.shape
+    qf = np.asfortranarray(q, dtype=np.float64)
+    qout = np.zeros_like(qf, order="F")
+    cfl = np.zeros(1)
+    lim = np.zeros(5, np.int32)
+    lim[:len(mthlim)] = mthlim
+    rc = lib3().gclaw3_ref_step_split(rp, _dp(_pd(pd)), mx, my, mz, _dp(qf), _dp(qout), dx, dy,
+                                      dz, dt, order, _ip(lim), _ip(np.array(bc_lower, np.int32)),
+                                      _ip(np.array(bc_upper, np.int32)), _dp(cfl), nthreads)
+    if rc < 0:
+        raise ValueError(f"gclaw3_ref_step_split failed: {rc}")
+    if rc:
+        raise FloatingPointError(f"gclaw3_ref_step_split: non-physical state ({rc})")
     return qout, float(cfl[0])

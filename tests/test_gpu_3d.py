@@ -1,12 +1,15 @@
-"""The unsplit 3D step (gclaw3_step / gclaw3_advance, acoustics_3D) on the
-GPU against the oracle's restatement of classic3.
+"""The 3D steps (gclaw3_step / gclaw3_advance and their split forms,
+acoustics_3D and euler_3D) on the GPU against the oracle's restatement of
+classic3.
 
 The -fmad=false build must reproduce the oracle bit for bit for every
 transverse option (0, 10, 11, 20, 22), order, limiter and boundary mix,
 including grids of 2 cells in a direction; the product build stays within
 1e-13 per step and FP32-bulk within 2e-6; device-controlled time stepping
 follows the oracle's evolve_to_time within 1e-12 (FP64) and 1e-6 (FP32);
-unknown transverse options and precisions are refused."""
+unknown transverse options and precisions are refused.  The dimensionally
+split step (ClawSolver3D's default) is held to the same bars against the
+oracle's split sweeps."""
 import ctypes
 import math
 
@@ -270,3 +273,101 @@ def test_euler_clawsolver3d_run(cuda, oracle):
     # mass and energy are conserved between walls
     for comp in (0, 4):
         assert abs(claw.frames[-1].q[comp].sum() - q0[comp].sum()) <= 1e-12 * q0[comp].sum()
+
+
+# ---------------------------------------------------------------------------
+# dimensionally split steps (gclaw3_step_split / gclaw3_advance_split)
+# ---------------------------------------------------------------------------
+def gpu_split3(rp, pd, q, d, dt, bcl, bcu, order=2, lim=4, strict=False, precision=0):
+    m, mx, my, mz = q.shape
+    s = make_solver3_struct(rp, mx, my, mz, *d, bcl, bcu, [lim] * 3, order, 22, precision, pd)
+    dev = DeviceProblem3(s, strict=strict, split=True)
+    dev.upload(q)
+    dev.step(dt, src=0)
+    c = dev.read_ctrl()
+    return dev.download(1), c
+
+
+@pytest.mark.parametrize("shape", [(2, 2, 2), (5, 4, 3), (17, 9, 12)])
+@pytest.mark.parametrize("bcl,bcu", BCS)
+@pytest.mark.parametrize("rp", [1, 2])
+def test_split_strict_bitwise(cuda, oracle, rp, shape, bcl, bcu):
+    rng = np.random.default_rng(11 * sum(shape) + bcl[0] + rp)
+    if rp == 1:
+        q, pd = np.asfortranarray(rng.normal(size=(4,) + shape)), PD3
+    else:
+        q, pd = euler3(shape, rng), [1.4]
+    d = (1.0 / shape[0], 1.1 / shape[1], 0.9 / shape[2])
+    dt = (0.05 if rp == 1 else 0.04) * min(d)
+    lim = [1, 2, 3, 4][sum(shape) % 4]
+    qo, cflo = oracle.step3_split(rp, pd, q, *d, dt, bcl, bcu, 2, [lim] * 3)
+    qs, c = gpu_split3(rp, pd, q, d, dt, bcl, bcu, lim=lim, strict=True)
+    assert c.status == 0
+    assert np.array_equal(qs, qo), np.abs(qs - qo).max()
+    assert c.cfl == cflo
+    qp, cp = gpu_split3(rp, pd, q, d, dt, bcl, bcu, lim=lim)
+    assert rel_l1(qp, qo) <= 1e-13 and abs(cp.cfl - cflo) <= 1e-14 * cflo
+    q32, c32 = gpu_split3(rp, pd, q, d, dt, bcl, bcu, lim=lim, precision=1)
+    assert rel_l1(q32, qo) <= 2e-6 and abs(c32.cfl - cflo) <= 1e-6 * cflo
+
+
+@pytest.mark.parametrize("order,lim", [(1, 0), (2, 1), (2, 0)])
+def test_split_options_strict_bitwise(cuda, oracle, order, lim):
+    rng = np.random.default_rng(order * 10 + lim)
+    q = np.asfortranarray(rng.normal(size=(4, 13, 11, 9)))
+    d = (0.1, 0.12, 0.09)
+    bcl, bcu = [3, 1, 2], [1, 3, 2]
+    qo, cflo = oracle.step3_split(1, PD3, q, *d, 0.02, bcl, bcu, order, [lim] * 3)
+    qs, c = gpu_split3(1, PD3, q, d, 0.02, bcl, bcu, order, lim, strict=True)
+    assert np.array_equal(qs, qo)
+    assert c.cfl == cflo
+
+
+def test_split_refusals(cuda):
+    L = _lib.lib()
+    s = make_solver3_struct(1, 8, 8, 8, 0.1, 0.1, 0.1, [1] * 3, [1] * 3, [4, 4], 2, 22, 0, PD3)
+    dev = DeviceProblem3(s, split=True)
+    p = [ctypes.c_void_p(t.data_ptr()) for t in (dev.q[0], dev.q[1], dev.qtmp)]
+    ws, ctrl = ctypes.c_void_p(dev.ws.data_ptr()), ctypes.c_void_p(dev.ctrl.data_ptr())
+    sp = ctypes.byref(s)
+    assert L.gclaw3_step_split(sp, p[0], p[1], p[0], 0.01, ws, ctrl, None) == _lib.ERR_ARG
+    assert L.gclaw3_step_split(sp, p[0], p[1], None, 0.01, ws, ctrl, None) == _lib.ERR_ARG
+    assert L.gclaw3_step_split(sp, p[0], p[1], p[2], 0.0, ws, ctrl, None) == _lib.ERR_ARG
+    assert L.gclaw3_advance_split(sp, p[0], p[1], p[1], ws, ctrl, 1, None) == _lib.ERR_ARG
+    assert L.gclaw3_advance_split(sp, p[0], p[1], p[2], ws, ctrl, -1, None) == _lib.ERR_ARG
+
+
+def test_split_clawsolver3d_run(cuda, oracle):
+    """ClawSolver3D's default (dimensional_split = True): an acoustic pulse
+    between mixed boundaries through the Controller against the oracle's
+    split steps under evolve_to_time."""
+    from clawpack_gb300 import pyclaw, riemann
+
+    dims = [pyclaw.Dimension(-1.0, 1.0, n, name=c) for n, c in ((20, "x"), (18, "y"), (16, "z"))]
+    domain = pyclaw.Domain(dims)
+    state = pyclaw.State(domain, 4)
+    state.problem_data.update(rho=1.0, bulk=4.0)
+    X, Y, Z = state.grid.p_centers
+    state.q[0] = np.exp(-20.0 * ((X - 0.2) ** 2 + Y ** 2 + (Z + 0.1) ** 2))
+    solver = pyclaw.ClawSolver3D(riemann.acoustics_3D)
+    assert solver.dimensional_split
+    solver.limiters = pyclaw.limiters.tvd.MC
+    solver.bc_lower = [pyclaw.BC.extrap, pyclaw.BC.wall, pyclaw.BC.periodic]
+    solver.bc_upper = [pyclaw.BC.extrap, pyclaw.BC.wall, pyclaw.BC.periodic]
+    solver.dt_initial = 0.01
+    claw = pyclaw.Controller()
+    claw.solution = pyclaw.Solution(state, domain)
+    claw.solver = solver
+    claw.tfinal, claw.num_output_times = 0.3, 3
+    q0 = state.q.copy()
+    claw.run()
+    d = tuple(state.grid.delta)
+    bcl, bcu = [1, 3, 2], [1, 3, 2]
+
+    def step(qq, dt):
+        return oracle.step3_split(1, PD3, qq, *d, dt, bcl, bcu, 2, [4, 4], nthreads=8)
+
+    q, t, dt = q0, 0.0, 0.01
+    for k in range(1, 4):
+        q, t, dt, _ = oracle.evolve(step, q, t, 0.1 * k, dt, cfl_desired=0.9, cfl_max=1.0)
+        assert rel_l1(claw.frames[k].q, q) <= 1e-12, k

@@ -125,8 +125,8 @@ def test_clawsolver3d_front_end():
     s = pyclaw.ClawSolver3D(riemann.acoustics_3D)
     assert s.transverse_waves == s.trans_cor == 22 and s.trans_inc == 11
     s.bc_lower = s.bc_upper = [pyclaw.BC.wall] * 3
-    with pytest.raises(NotImplementedError):  # 3D steps are unsplit here
-        s.solver_struct(st)
+    assert s.dimensional_split  # split sweeps by default, unsplit on request
+    s.solver_struct(st)
     s.dimensional_split = False
     ss = s.solver_struct(st)
     assert (ss.mx, ss.my, ss.mz) == (8, 6, 5) and list(ss.problem_data)[:4] == [1, 4, 2, 2]
