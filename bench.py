@@ -357,12 +357,35 @@ def bench_euler(args, torch, world, device):
 
 
 def bench_3d(args, torch, world, device):
-    """Unsplit 3D step (classic3, acoustics_3D, transverse_waves 22, MC):
-    a pressure pulse between walls on an n^3 cube, FP64, 40 device-controlled
-    steps (1.7 GB of state and workspace per 192^3, above L2), and the CPU
-    oracle on a 48^3 cube for reference."""
+    """3D steps (classic3, acoustics_3D, MC): a pressure pulse between walls
+    on an n^3 cube, unsplit with transverse_waves 22 and dimensionally split,
+    FP64 and FP32-bulk, 40 device-controlled steps each (1.7 GB of state and
+    workspace per 192^3, above L2); euler_3D on the octant problem; and the
+    CPU oracle on a 48^3 cube for reference."""
     from clawpack_gb300 import workloads
     from clawpack_gb300.device import DeviceProblem3
+
+    def timed(make, n, k, prec, split=False):
+        # a 32^3 warm-up run of the same kernels, then k device-controlled
+        # steps on the n^3 problem
+        for prob, kk in ((make(32), 3), (make(n), k)):
+            dev = DeviceProblem3(prob.solver_struct(precision=prec), device=device, split=split)
+            dev.upload(prob.q0)
+            dev.ctrl_init(0.0, prob.dt_initial, math.inf, cfl_max=prob.cfl_max,
+                          cfl_desired=prob.cfl_desired, max_accepted=kk, max_steps=10 * kk)
+            torch.cuda.synchronize()
+            barrier(world)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dev.advance(kk)
+            e1.record()
+            torch.cuda.synchronize()
+            secs = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world, device)
+            c = dev.read_ctrl()
+        res = {"value": round(world * n ** 3 * c.numsteps / secs * 1e-9, 4),
+               "ms_per_step": round(secs / k * 1e3, 3),
+               "accepted_steps": int(c.numsteps), "status": int(c.status)}
+        return res, dev.q[c.parity].clone()
 
     n, steps = args.n3d, 40
     out = {"workload": f"acoustics_3d_pulse {n}^3, wall BCs, MC, transverse_waves 22 "
@@ -370,53 +393,22 @@ def bench_3d(args, torch, world, device):
            "unit": UNIT, "launches": 2 * 9 * (steps + 3)}
     finals = {}
     for name, prec in (("fp64", 0), ("fp32_bulk", 1)):
-        for prob, k in ((workloads.acoustics_3d_pulse(32), 3),
-                        (workloads.acoustics_3d_pulse(n), steps)):
-            dev = DeviceProblem3(prob.solver_struct(precision=prec), device=device)
-            dev.upload(prob.q0)
-            dev.ctrl_init(0.0, prob.dt_initial, math.inf, cfl_max=prob.cfl_max,
-                          cfl_desired=prob.cfl_desired, max_accepted=k, max_steps=10 * k)
-            torch.cuda.synchronize()
-            barrier(world)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            dev.advance(k)
-            e1.record()
-            torch.cuda.synchronize()
-            secs = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world, device)
-            c = dev.read_ctrl()
-        out[name] = {"value": round(world * n ** 3 * c.numsteps / secs * 1e-9, 4),
-                     "ms_per_step": round(secs / steps * 1e3, 3),
-                     "accepted_steps": int(c.numsteps), "status": int(c.status)}
-        finals[name] = dev.q[c.parity].clone()
-        del dev
+        out[name], finals[name] = timed(workloads.acoustics_3d_pulse, n, steps, prec)
     a, b = finals["fp32_bulk"], finals["fp64"]
     out["fp32_rel_l1_vs_fp64"] = float((a - b).abs().sum() / b.abs().sum())
+    # ClawSolver3D's default: dimensionally split sweeps, same problem
+    out["split"] = {"workload": f"acoustics_3d_pulse {n}^3, dimensionally split, MC, "
+                                f"{steps} steps"}
+    for name, prec in (("fp64", 0), ("fp32_bulk", 1)):
+        out["split"][name], _ = timed(workloads.acoustics_3d_pulse, n, steps, prec, split=True)
+    out["launches"] += 2 * 9 * (steps + 3)
     # 3D Euler (euler_3D, Roe, three wave families) on the seeded octant
     # problem, 128^3, extrapolation boundaries, MC limiter, CFL 0.8
     ne, esteps = 128, 20
     eu = {"workload": f"euler_3d_octants {ne}^3 (seed {workloads.EULER3D_SEED}), extrap BCs, "
                       f"MC, transverse_waves 22, CFL 0.8, {esteps} steps"}
     for name, prec in (("fp64", 0), ("fp32_bulk", 1)):
-        for prob, k in ((workloads.euler_3d_octants(32), 3),
-                        (workloads.euler_3d_octants(ne), esteps)):
-            dev = DeviceProblem3(prob.solver_struct(precision=prec), device=device)
-            dev.upload(prob.q0)
-            dev.ctrl_init(0.0, prob.dt_initial, math.inf, cfl_max=prob.cfl_max,
-                          cfl_desired=prob.cfl_desired, max_accepted=k, max_steps=10 * k)
-            torch.cuda.synchronize()
-            barrier(world)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            dev.advance(k)
-            e1.record()
-            torch.cuda.synchronize()
-            secs = max_over_ranks(e0.elapsed_time(e1) * 1e-3, world, device)
-            c = dev.read_ctrl()
-        eu[name] = {"value": round(world * ne ** 3 * c.numsteps / secs * 1e-9, 4),
-                    "ms_per_step": round(secs / esteps * 1e3, 3),
-                    "accepted_steps": int(c.numsteps), "status": int(c.status)}
-        del dev
+        eu[name], _ = timed(workloads.euler_3d_octants, ne, esteps, prec)
     out["euler_3d"] = eu
     out["launches"] += 2 * 9 * (esteps + 3)
     if int(os.environ.get("RANK", "0")) == 0:

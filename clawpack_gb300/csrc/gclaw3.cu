@@ -32,6 +32,24 @@ namespace g3 {
 
 constexpr int NT3 = 256;
 
+// Division of a 32-bit index by a runtime divisor d >= 2 as a multiply-high
+// and a shift (Granlund and Montgomery, PLDI 1994): with l = ceil(log2 d)
+// and m = ceil(2^(31 + l) / d), which is below 2^32, floor(n / d) equals
+// umulhi(n, m) >> (l - 1) for every n < 2^31.
+struct Divisor {
+    unsigned m;
+    int s, d;
+};
+static Divisor make_divisor(int d) {
+    int l = 0;
+    while ((1ll << l) < d) l++;
+    const unsigned long long m = ((1ull << (31 + l)) + (unsigned long long)d - 1) / d;
+    return Divisor{(unsigned)m, l - 1, d};
+}
+__device__ __forceinline__ unsigned udiv(unsigned n, const Divisor &v) {
+    return __umulhi(n, v.m) >> v.s;
+}
+
 struct Args3 {
     const double *qin[2];
     double *qout[2];
@@ -43,8 +61,17 @@ struct Args3 {
     int n[3];
     int bc_lo[3], bc_hi[3];
     int mthlim, order, tw, ctrl_mode;
-    long long npos;  // edge-box positions (n0 + 3)(n1 + 3)(n2 + 3)
+    long long npos;  // edge-box positions (n0 + 3)(n1 + 3)(n2 + 3), below 2^31
+    Divisor box_x, box_y, cell_x, cell_y;  // n0 + 3, n1 + 3, n0, n1
 };
+
+// Box position idx -> (x, y, z), each in [-1, n + 1].
+__device__ __forceinline__ void box_coords(const Args3 &a, unsigned idx, int p[3]) {
+    const unsigned r = udiv(idx, a.box_x), z = udiv(r, a.box_y);
+    p[0] = (int)(idx - r * (unsigned)a.box_x.d) - 1;
+    p[1] = (int)(r - z * (unsigned)a.box_y.d) - 1;
+    p[2] = (int)z - 1;
+}
 
 // Constant-coefficient acoustics, q = (p, u, v, w); the velocity along axis
 // a is q[1 + a] (upstream riemann rpn3/rpt3/rptt3_acoustics.f90).
@@ -359,11 +386,8 @@ __global__ void __launch_bounds__(NT3) k_edges(const Args3 a, const typename RPT
     bool bad = false;
     const long long idx = (long long)blockIdx.x * NT3 + threadIdx.x;
     if (idx < a.npos) {
-        const int X = a.n[0] + 3, Y = a.n[1] + 3;
         int p[3];
-        p[0] = (int)(idx % X) - 1;
-        p[1] = (int)((idx / X) % Y) - 1;
-        p[2] = (int)(idx / ((long long)X * Y)) - 1;
+        box_coords(a, (unsigned)idx, p);
         int l[3] = {p[0], p[1], p[2]};
         l[D] -= 1;
         T ql[M], qr[M];
@@ -385,8 +409,9 @@ __global__ void __launch_bounds__(NT3) k_edges(const Args3 a, const typename RPT
             ws[(F::AM + k) * np + idx] = am[k];
             ws[(F::AP + k) * np + idx] = ap[k];
         }
+        if (a.tw)  // the edge state only feeds the transverse chains
 #pragma unroll
-        for (int r = 0; r < RP::NR; r++) ws[(F::R + r) * np + idx] = R[r];
+            for (int r = 0; r < RP::NR; r++) ws[(F::R + r) * np + idx] = R[r];
         // Courant numbers of the edges 0..n along the sweep in every slice
         // (ghost slices included, as the serial sweep counts them)
         // non-physical states on any edge of the slices the sweep uses
@@ -473,7 +498,9 @@ __device__ __forceinline__ void chain(const typename RP::Params &P, const T *R, 
             }
 }
 
-template <template <typename> class RPT, int D, typename T>
+// TR: transverse terms present (transverse_waves != 0); without them the
+// kernel is the limiter alone, compiled without the chain code.
+template <template <typename> class RPT, int D, typename T, bool TR>
 __global__ void __launch_bounds__(NT3) k_chains(const Args3 a, const typename RPT<T>::Params P) {
     using RP = RPT<T>;
     using F = Fields<RP>;
@@ -485,11 +512,11 @@ __global__ void __launch_bounds__(NT3) k_chains(const Args3 a, const typename RP
     if (idx >= a.npos) return;
     const int X = a.n[0] + 3, Y = a.n[1] + 3;
     int p[3];
-    p[0] = (int)(idx % X) - 1;
-    p[1] = (int)((idx / X) % Y) - 1;
-    p[2] = (int)(idx / ((long long)X * Y)) - 1;
-    // edges 0..n along the sweep, slices -1..n across it
+    box_coords(a, (unsigned)idx, p);
+    // edges 0..n along the sweep, slices -1..n across it (0..n-1 without
+    // transverse terms: no chain reaches into a neighbouring slice)
     if (p[D] < 0 || p[D] > a.n[D] || p[T1] > a.n[T1] || p[T2] > a.n[T2]) return;
+    if (!TR && (p[T1] < 0 || p[T2] < 0 || p[T1] == a.n[T1] || p[T2] == a.n[T2])) return;
     T *ws = static_cast<T *>(a.ws);
     const long long np = a.npos;
     long long stepd = 1;
@@ -546,6 +573,7 @@ __global__ void __launch_bounds__(NT3) k_chains(const Args3 a, const typename RP
 #pragma unroll
     for (int k = 0; k < M; k++) ws[(F::FA + k) * np + idx] = (T)0 + (T)0.5 * cq[k];
 
+    if (!TR) return;
     const int single = a.tw / 10;
     const bool dbl = (a.tw % 10) > 0;
     T am[M], ap[M];
@@ -567,20 +595,16 @@ __global__ void __launch_bounds__(NT3) k_chains(const Args3 a, const typename RP
         for (int r = 0; r < RP::NR; r++) R[r] = ws[(F::R + r) * np + idx];
         chain<RP, D, T>(P, R, am, dbl, h, f1, f2, ws, np, idx, F::AMC);
         chain<RP, D, T>(P, R, ap, dbl, h, f1, f2, ws, np, idx, F::APC);
-    } else {
-#pragma unroll
-        for (int e = 0; e < F::NCH; e++) {
-            ws[(long long)(F::AMC + e) * np + idx] = (T)0;
-            ws[(long long)(F::APC + e) * np + idx] = (T)0;
-        }
     }
+    // without transverse terms (transverse_waves 0, and every split sweep)
+    // the chain slots are neither written nor read
 }
 
 // ---- k_update: per-cell accumulation of one sweep ---------------------------
 // FP64: the terms are added to the state itself, in the oracle's order.
 // FP32-bulk: they are summed in FP32 from zero and the sum is added to the
 // FP64 state once.
-template <template <typename> class RPT, int D, typename T>
+template <template <typename> class RPT, int D, typename T, bool TR>
 __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
     using RP = RPT<T>;
     using F = Fields<RP>;
@@ -593,9 +617,10 @@ __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
     const long long cid = (long long)blockIdx.x * NT3 + threadIdx.x;
     if (cid < ncell) {
         int p[3];
-        p[0] = (int)(cid % a.n[0]);
-        p[1] = (int)((cid / a.n[0]) % a.n[1]);
-        p[2] = (int)(cid / ((long long)a.n[0] * a.n[1]));
+        const unsigned r = udiv((unsigned)cid, a.cell_x), z = udiv(r, a.cell_y);
+        p[0] = (int)((unsigned)cid - r * (unsigned)a.n[0]);
+        p[1] = (int)(r - z * (unsigned)a.n[1]);
+        p[2] = (int)z;
         // the x-sweep starts from the old state, the others add to the new
         // one (unsplit) or start from the previous sweep's result (split)
         const double *src = a.split ? sweep_in(a, D, L.par) : D == 0 ? a.qin[L.par] : a.qout[L.par];
@@ -608,6 +633,23 @@ __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
 #pragma unroll
         for (int k = 0; k < M; k++) v[k] = F64 ? (T)src[o + k] : (T)0;
         const int c = p[D], A = p[T1], B = p[T2];
+        if (!TR) {
+            // no chains: the transverse entries are all +0, which leaves the
+            // normal update and, from the eight other slices, a +0 that turns
+            // a -0 into +0 as the full gather does
+            const long long i0 = bpos(a, p[0], p[1], p[2]);
+            int e1[3] = {p[0], p[1], p[2]};
+            e1[D] = c + 1;
+            const long long i1 = bpos(a, e1[0], e1[1], e1[2]);
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                const T qa = ((T)0 - dtn * ws[(F::AP + k) * np + i0]) -
+                             dtn * ws[(F::AM + k) * np + i1];
+                const T fa0 = ws[(F::FA + k) * np + i0];
+                const T fa1 = ws[(F::FA + k) * np + i1];
+                v[k] = (v[k] + qa - dtn * (fa1 - fa0)) + (T)0;
+            }
+        } else
 #pragma unroll
         for (int db = -1; db <= 1; db++)
 #pragma unroll
@@ -676,8 +718,13 @@ static int sweep(const gclaw3_solver *s, const Args3 &a, cudaStream_t st) {
     const long long ncell = (long long)s->mx * s->my * s->mz;
     const unsigned nc = (unsigned)((ncell + NT3 - 1) / NT3);
     k_edges<RPT, D, T><<<nb, NT3, 0, st>>>(a, P);
-    k_chains<RPT, D, T><<<nb, NT3, 0, st>>>(a, P);
-    k_update<RPT, D, T><<<nc, NT3, 0, st>>>(a);
+    if (a.tw) {
+        k_chains<RPT, D, T, true><<<nb, NT3, 0, st>>>(a, P);
+        k_update<RPT, D, T, true><<<nc, NT3, 0, st>>>(a);
+    } else {
+        k_chains<RPT, D, T, false><<<nb, NT3, 0, st>>>(a, P);
+        k_update<RPT, D, T, false><<<nc, NT3, 0, st>>>(a);
+    }
     return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
 }
 
@@ -719,6 +766,10 @@ static void fill_args(const gclaw3_solver *s, Args3 &a) {
     a.order = s->order;
     a.tw = s->transverse_waves;
     a.npos = box_positions(s);
+    a.box_x = make_divisor(s->mx + 3);
+    a.box_y = make_divisor(s->my + 3);
+    a.cell_x = make_divisor(s->mx);
+    a.cell_y = make_divisor(s->my);
 }
 
 }  // namespace g3
@@ -742,7 +793,9 @@ int gclaw3_check(const gclaw3_solver *s) {
     if (!s || gclaw3_rp_shape(s->rp, &m, &mw)) return GCLAW_ERR_ARG;
     if (s->mx < 2 || s->my < 2 || s->mz < 2) return GCLAW_ERR_ARG;
     if (!(s->dx > 0.0) || !(s->dy > 0.0) || !(s->dz > 0.0)) return GCLAW_ERR_ARG;
-    if ((double)(s->mx + 3) * (s->my + 3) * (s->mz + 3) > 4.0e9) return GCLAW_ERR_ARG;
+    // 32-bit position arithmetic (the workspace of a larger box would not
+    // fit in HBM anyway)
+    if ((double)(s->mx + 3) * (s->my + 3) * (s->mz + 3) >= 2147483648.0) return GCLAW_ERR_ARG;
     for (int d = 0; d < 3; d++) {
         if (s->bc_lower[d] == GCLAW_BC_CUSTOM || s->bc_upper[d] == GCLAW_BC_CUSTOM)
             return GCLAW_ERR_UNSUPPORTED;

@@ -86,7 +86,8 @@ def run_3d(a):
 
     w = (workloads.acoustics_3d_pulse(a.mx) if a.workload == "acoustics3d"
          else workloads.euler_3d_octants(a.mx))
-    dev = DeviceProblem3(w.solver_struct(precision=0 if a.precision == "fp64" else 1))
+    dev = DeviceProblem3(w.solver_struct(precision=0 if a.precision == "fp64" else 1),
+                         split=a.split)
     dev.upload(w.q0)
     dev.ctrl_init(0.0, w.dt_initial, math.inf, cfl_max=w.cfl_max, cfl_desired=w.cfl_desired,
                   max_steps=10 ** 9)
@@ -99,7 +100,8 @@ def run_3d(a):
     c = dev.read_ctrl()
     ms = e0.elapsed_time(e1) / max(a.steps, 1)
     cells = w.n ** 3
-    print(json.dumps({"workload": w.name, "n": w.n, "precision": a.precision, "steps": a.steps,
+    print(json.dumps({"workload": w.name, "n": w.n, "precision": a.precision, "split": a.split,
+                      "steps": a.steps,
                       "ms_per_step": ms,
                       "gcell_updates_per_s": cells / (ms * 1e-3) * 1e-9 if ms > 0 else None,
                       "accepted": c.numsteps, "status": c.status, "cfl": c.cfl}))

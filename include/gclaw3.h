@@ -34,7 +34,8 @@ extern "C" {
 
 typedef struct gclaw3_solver {
     int rp;                       /* GCLAW3_RP_* */
-    int mx, my, mz;               /* interior cells, each >= 2 */
+    int mx, my, mz;               /* interior cells, each >= 2,
+                                     (mx + 3)(my + 3)(mz + 3) < 2^31 */
     double dx, dy, dz;
     int bc_lower[3], bc_upper[3]; /* GCLAW_BC_EXTRAP / PERIODIC / WALL per axis */
     int mthlim[GCLAW_MAX_WAVES];  /* limiter per wave family */
