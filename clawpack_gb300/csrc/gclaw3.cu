@@ -63,6 +63,8 @@ struct Args3 {
     int mthlim, order, tw, ctrl_mode;
     long long npos;  // edge-box positions (n0 + 3)(n1 + 3)(n2 + 3), below 2^31
     Divisor box_x, box_y, cell_x, cell_y;  // n0 + 3, n1 + 3, n0, n1
+    Divisor pen0, pen1;  // k_pencil: cells along its two pencil axes
+    long long npen;      // k_pencil: threads (pencils x chunks)
 };
 
 // Box position idx -> (x, y, z), each in [-1, n + 1].
@@ -336,6 +338,77 @@ __device__ __forceinline__ double load_q3(const Args3 &a, const double *__restri
                                 (neg ? (long long)0x8000000000000000ull : 0ll));
 }
 
+// The M components of cell (g0, g1, g2) whose coordinates across axis D are
+// interior and whose g[D] is in [-2, n+1], through the boundary conditions
+// along D (the mapping of load_q3 for such cells, done once per cell), and
+// converted to T.  Cells of an even number of components are 16-byte
+// aligned and load as double2.
+template <int M, int D, typename T>
+__device__ __forceinline__ void load_pencil(const Args3 &a, const double *__restrict__ q, int g0,
+                                            int g1, int g2, T *out) {
+    int g[3] = {g0, g1, g2};
+    const int n = a.n[D];
+    int v = min(max(g[D], -2), n + 1);
+    bool wall = false;
+    if (v < 0) {
+        const int b = a.bc_lo[D];
+        if (b == GCLAW_BC_EXTRAP) v = 0;
+        else if (b == GCLAW_BC_PERIODIC) v = v + n;
+        else { v = -1 - v; wall = true; }
+    } else if (v >= n) {
+        const int b = a.bc_hi[D];
+        if (b == GCLAW_BC_EXTRAP) v = n - 1;
+        else if (b == GCLAW_BC_PERIODIC) v = v - n;
+        else { v = 2 * n - 1 - v; wall = true; }
+    }
+    g[D] = v;
+    const double *c = q + (size_t)M * ((size_t)g[0] + (size_t)a.n[0] *
+                                       ((size_t)g[1] + (size_t)a.n[1] * (size_t)g[2]));
+    double x[M];
+    if (M % 2 == 0) {
+#pragma unroll
+        for (int k = 0; k < M; k += 2) {
+            const double2 u = __ldg(reinterpret_cast<const double2 *>(c + k));
+            x[k] = u.x;
+            x[k + 1] = u.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < M; k++) x[k] = __ldg(c + k);
+    }
+    if (M > 1 + D && wall) x[1 + D] = __longlong_as_double(__double_as_longlong(x[1 + D]) ^
+                                                          (long long)0x8000000000000000ull);
+#pragma unroll
+    for (int k = 0; k < M; k++) out[k] = from_double<T>(x[k]);
+}
+
+// M doubles to cell offset o (16-byte aligned when M is even)
+template <int M>
+__device__ __forceinline__ void store_cell(double *dst, size_t o, const double *v) {
+    if (M % 2 == 0) {
+#pragma unroll
+        for (int k = 0; k < M; k += 2)
+            *reinterpret_cast<double2 *>(dst + o + k) = make_double2(v[k], v[k + 1]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < M; k++) dst[o + k] = v[k];
+    }
+}
+template <int M>
+__device__ __forceinline__ void load_cell(const double *src, size_t o, double *v) {
+    if (M % 2 == 0) {
+#pragma unroll
+        for (int k = 0; k < M; k += 2) {
+            const double2 u = *reinterpret_cast<const double2 *>(src + o + k);
+            v[k] = u.x;
+            v[k + 1] = u.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < M; k++) v[k] = src[o + k];
+    }
+}
+
 // The state a sweep starts from and the one it writes.  Unsplit: every
 // sweep reads the old state, the x-sweep writes the new one and the others
 // add to it.  Split (x, y, z in turn): old -> new -> tmp -> new.
@@ -409,9 +482,8 @@ __global__ void __launch_bounds__(NT3) k_edges(const Args3 a, const typename RPT
             ws[(F::AM + k) * np + idx] = am[k];
             ws[(F::AP + k) * np + idx] = ap[k];
         }
-        if (a.tw)  // the edge state only feeds the transverse chains
 #pragma unroll
-            for (int r = 0; r < RP::NR; r++) ws[(F::R + r) * np + idx] = R[r];
+        for (int r = 0; r < RP::NR; r++) ws[(F::R + r) * np + idx] = R[r];
         // Courant numbers of the edges 0..n along the sweep in every slice
         // (ghost slices included, as the serial sweep counts them)
         // non-physical states on any edge of the slices the sweep uses
@@ -498,9 +570,7 @@ __device__ __forceinline__ void chain(const typename RP::Params &P, const T *R, 
             }
 }
 
-// TR: transverse terms present (transverse_waves != 0); without them the
-// kernel is the limiter alone, compiled without the chain code.
-template <template <typename> class RPT, int D, typename T, bool TR>
+template <template <typename> class RPT, int D, typename T>
 __global__ void __launch_bounds__(NT3) k_chains(const Args3 a, const typename RPT<T>::Params P) {
     using RP = RPT<T>;
     using F = Fields<RP>;
@@ -513,10 +583,8 @@ __global__ void __launch_bounds__(NT3) k_chains(const Args3 a, const typename RP
     const int X = a.n[0] + 3, Y = a.n[1] + 3;
     int p[3];
     box_coords(a, (unsigned)idx, p);
-    // edges 0..n along the sweep, slices -1..n across it (0..n-1 without
-    // transverse terms: no chain reaches into a neighbouring slice)
+    // edges 0..n along the sweep, slices -1..n across it
     if (p[D] < 0 || p[D] > a.n[D] || p[T1] > a.n[T1] || p[T2] > a.n[T2]) return;
-    if (!TR && (p[T1] < 0 || p[T2] < 0 || p[T1] == a.n[T1] || p[T2] == a.n[T2])) return;
     T *ws = static_cast<T *>(a.ws);
     const long long np = a.npos;
     long long stepd = 1;
@@ -573,7 +641,6 @@ __global__ void __launch_bounds__(NT3) k_chains(const Args3 a, const typename RP
 #pragma unroll
     for (int k = 0; k < M; k++) ws[(F::FA + k) * np + idx] = (T)0 + (T)0.5 * cq[k];
 
-    if (!TR) return;
     const int single = a.tw / 10;
     const bool dbl = (a.tw % 10) > 0;
     T am[M], ap[M];
@@ -596,15 +663,13 @@ __global__ void __launch_bounds__(NT3) k_chains(const Args3 a, const typename RP
         chain<RP, D, T>(P, R, am, dbl, h, f1, f2, ws, np, idx, F::AMC);
         chain<RP, D, T>(P, R, ap, dbl, h, f1, f2, ws, np, idx, F::APC);
     }
-    // without transverse terms (transverse_waves 0, and every split sweep)
-    // the chain slots are neither written nor read
 }
 
 // ---- k_update: per-cell accumulation of one sweep ---------------------------
 // FP64: the terms are added to the state itself, in the oracle's order.
 // FP32-bulk: they are summed in FP32 from zero and the sum is added to the
 // FP64 state once.
-template <template <typename> class RPT, int D, typename T, bool TR>
+template <template <typename> class RPT, int D, typename T>
 __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
     using RP = RPT<T>;
     using F = Fields<RP>;
@@ -633,23 +698,6 @@ __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
 #pragma unroll
         for (int k = 0; k < M; k++) v[k] = F64 ? (T)src[o + k] : (T)0;
         const int c = p[D], A = p[T1], B = p[T2];
-        if (!TR) {
-            // no chains: the transverse entries are all +0, which leaves the
-            // normal update and, from the eight other slices, a +0 that turns
-            // a -0 into +0 as the full gather does
-            const long long i0 = bpos(a, p[0], p[1], p[2]);
-            int e1[3] = {p[0], p[1], p[2]};
-            e1[D] = c + 1;
-            const long long i1 = bpos(a, e1[0], e1[1], e1[2]);
-#pragma unroll
-            for (int k = 0; k < M; k++) {
-                const T qa = ((T)0 - dtn * ws[(F::AP + k) * np + i0]) -
-                             dtn * ws[(F::AM + k) * np + i1];
-                const T fa0 = ws[(F::FA + k) * np + i0];
-                const T fa1 = ws[(F::FA + k) * np + i1];
-                v[k] = (v[k] + qa - dtn * (fa1 - fa0)) + (T)0;
-            }
-        } else
 #pragma unroll
         for (int db = -1; db <= 1; db++)
 #pragma unroll
@@ -711,20 +759,349 @@ __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
     }
 }
 
+// ---- k_pencil: a whole sweep without transverse terms ----------------------
+// Without transverse terms (every dimensionally split sweep, and
+// transverse_waves 0) a sweep is a set of independent 1D problems along its
+// axis.  Each thread marches along a chunk of pencil_len cells (16 in FP32,
+// 32 in FP64) of one pencil with
+// the unlimited waves of three consecutive edges in registers: it solves the
+// edge two ahead of the cell, limits the edge after the cell and updates the
+// cell.  The state is read once (plus a four-cell overlap per chunk) and
+// written once, and no edge record goes to HBM.  The arithmetic and its
+// order are those of k_edges, k_chains and k_update without transverse
+// terms.  Pencils of the ghost slices across the sweep are not visited:
+// with extrapolation, periodic and wall boundaries their states are interior
+// states with a transverse velocity negated, whose normal Riemann problems
+// have the same speeds and the same physicality, so the Courant number and
+// the status flags come out the same.
+// limited correction flux fa = 0 + 0.5 cq of the edge with unlimited waves
+// Wc and speeds s, between the edges with waves Wl (before) and Wr (after)
+template <class RP, typename T>
+__device__ __forceinline__ void limit_edge(const Args3 &a, const T *Wl, const T *Wc, const T *Wr,
+                                           const T *s, T dtdn, T *fa) {
+    constexpr int M = RP::M, MW = RP::MW;
+    T W[MW * M], cq[M];
+#pragma unroll
+    for (int f = 0; f < MW * M; f++) W[f] = Wc[f];
+#pragma unroll
+    for (int k = 0; k < M; k++) cq[k] = (T)0;
+    if (a.order == 2) {
+#pragma unroll
+        for (int q = 0; q < MW; q++) {
+            const int lim = (a.mthlim >> (8 * q)) & 0xff;
+            if (lim == 0) continue;
+            T wn2 = (T)0;
+#pragma unroll
+            for (int k = 0; k < M; k++) wn2 = wn2 + W[q * M + k] * W[q * M + k];
+            if (eq0(wn2)) continue;
+            T dot = (T)0;
+            if (gt0(s[q])) {
+#pragma unroll
+                for (int k = 0; k < M; k++) dot = dot + Wl[q * M + k] * W[q * M + k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < M; k++) dot = dot + W[q * M + k] * Wr[q * M + k];
+            }
+            T phi = (T)0;
+            if (!le0(dot)) {
+                const T th = qdiv(dot, wn2);
+                phi = gt0(th) ? philim_pos<T>(lim, th) : philim<T>(lim, th);
+            }
+#pragma unroll
+            for (int k = 0; k < M; k++) W[q * M + k] = phi * W[q * M + k];
+        }
+        const T dtave = (T)0.5 * (dtdn + dtdn);
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            T c = (T)0;
+#pragma unroll
+            for (int q = 0; q < MW; q++) {
+                const T sa = tabs(s[q]);
+                c = c + sa * ((T)1 - sa * dtave) * W[q * M + k];
+            }
+            cq[k] = c;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < M; k++) fa[k] = (T)0 + (T)0.5 * cq[k];
+}
+
+// dt / d (rounded to T) once per block: an FP64 division per thread would
+// occupy the narrow FP64 pipe of GB300 out of proportion to the sweep
+template <typename T>
+__device__ __forceinline__ T block_dtd(double dt, double d) {
+    __shared__ T s_v;
+    if (threadIdx.x == 0) s_v = (T)(dt / d);
+    __syncthreads();
+    return s_v;
+}
+
+// blocks per SM the marching kernel is compiled for: four (64 registers)
+// for FP32 acoustics, one for FP64 Euler, whose three-edge window needs the
+// whole register file, two (128 registers) otherwise
+template <template <typename> class RPT, typename T>
+constexpr int pencil_blocks() {
+    return sizeof(T) == 8 ? (RPT<T>::M > 4 ? 1 : 2) : (RPT<T>::M > 4 ? 2 : 4);
+}
+// cells per chunk of the marching kernel: longer chunks in FP64, where the
+// overlap's extra Riemann problems cost FP64-pipe time, shorter in FP32 for
+// more threads in flight
+template <typename T>
+__host__ __device__ constexpr int pencil_len() { return sizeof(T) == 8 ? 32 : 16; }
+
+template <template <typename> class RPT, int D, typename T>
+__global__ void __launch_bounds__(NT3, pencil_blocks<RPT, T>()) k_pencil(const Args3 a, const typename RPT<T>::Params P) {
+    using RP = RPT<T>;
+    constexpr int M = RP::M, MW = RP::MW, NR = RP::NR > 0 ? RP::NR : 1;
+    constexpr int A0 = D == 0 ? 1 : 0, A1 = D == 2 ? 1 : 2;
+    constexpr bool F64 = sizeof(T) == 8;
+    const Launch L = launch_state(a);
+    if (L.skip) return;
+    const double *__restrict__ qin = sweep_in(a, D, L.par);
+    const double *src = a.split ? sweep_in(a, D, L.par) : D == 0 ? a.qin[L.par] : a.qout[L.par];
+    double *dst = sweep_out(a, D, L.par);
+    const T dtdn = block_dtd<T>(L.dt, a.d[D]);
+    T cmax = (T)0;
+    bool bad = false;
+    const long long t = (long long)blockIdx.x * NT3 + threadIdx.x;
+    if (t < a.npen) {
+        int p[3];
+        const unsigned r = udiv((unsigned)t, a.pen0), ch = udiv(r, a.pen1);
+        p[A0] = (int)((unsigned)t - r * (unsigned)a.n[A0]);
+        p[A1] = (int)(r - ch * (unsigned)a.n[A1]);
+        const int n = a.n[D];
+        constexpr int PL = pencil_len<T>();
+        const int c0 = (int)ch * PL, c1 = min(c0 + PL, n);
+        T qa[M], qb[M], R[NR], am[M], ap[M];
+        T Wp[MW * M], Wc[MW * M], Wn[MW * M], Wx[MW * M];
+        T sc[MW], sn[MW], sx[MW];
+        T apc[M], amn[M], apn[M], fa0[M], fa1[M];
+        // solve the edge e between cells e - 1 (ql) and e (qr), with the
+        // Courant-number and flag bookkeeping of k_edges
+        auto solve = [&](int e, const T *ql, const T *qr, T *W, T *sp, T *amo, T *apo) {
+            const bool eb = RP::template rpn3<D>(P, ql, qr, W, sp, amo, apo, R);
+            bad |= eb;
+            if (e >= 0 && e <= n) {
+#pragma unroll
+                for (int q = 0; q < MW; q++) {
+                    bad |= isnan_v(sp[q]);
+                    cmax = max_abs(cmax, dtdn * sp[q]);
+                }
+            }
+        };
+        auto load = [&](int c, T *q) {
+            int g[3] = {p[0], p[1], p[2]};
+            g[D] = c;
+            load_pencil<M, D, T>(a, qin, g[0], g[1], g[2], q);
+        };
+        load(c0 - 2, qa);
+        load(c0 - 1, qb);
+        solve(c0 - 1, qa, qb, Wp, sx, am, ap);
+        load(c0, qa);
+        solve(c0, qb, qa, Wc, sc, am, apc);
+        load(c0 + 1, qb);
+        solve(c0 + 1, qa, qb, Wn, sn, amn, apn);
+        limit_edge<RP, T>(a, Wp, Wc, Wn, sc, dtdn, fa0);
+        // qb holds the cell after the current one; the cell after that is
+        // loaded an iteration ahead, so its latency overlaps the arithmetic
+        T qf[M];
+        load(c0 + 2, qf);
+#pragma unroll 1
+        for (int c = c0; c < c1; c++) {
+#pragma unroll
+            for (int k = 0; k < M; k++) qa[k] = qf[k];
+            if (c + 1 < c1) load(c + 3, qf);
+            solve(c + 2, qb, qa, Wx, sx, am, ap);
+            limit_edge<RP, T>(a, Wc, Wn, Wx, sn, dtdn, fa1);
+            int g[3] = {p[0], p[1], p[2]};
+            g[D] = c;
+            const size_t o = (size_t)M * ((size_t)g[0] + (size_t)a.n[0] *
+                                          ((size_t)g[1] + (size_t)a.n[1] * (size_t)g[2]));
+            double q0[M];
+            load_cell<M>(src, o, q0);
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                const T qd = ((T)0 - dtdn * apc[k]) - dtdn * amn[k];
+                T v = F64 ? (T)q0[k] : (T)0;
+                v = (v + qd - dtdn * (fa1[k] - fa0[k])) + (T)0;
+                q0[k] = F64 ? (double)v : q0[k] + f2d_bits((float)v);
+            }
+            store_cell<M>(dst, o, q0);
+#pragma unroll
+            for (int f = 0; f < MW * M; f++) {
+                Wc[f] = Wn[f];
+                Wn[f] = Wx[f];
+            }
+#pragma unroll
+            for (int q = 0; q < MW; q++) sn[q] = sx[q];
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                apc[k] = apn[k];
+                amn[k] = am[k];
+                apn[k] = ap[k];
+                fa0[k] = fa1[k];
+                qb[k] = qa[k];
+            }
+        }
+    }
+    // block max and flag, then one atomic each
+    __shared__ T s_red[NT3 / 32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) cmax = tmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = cmax;
+    const int any = __syncthreads_or(bad ? 1 : 0);
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < NT3 / 32; w++) cmax = tmax(cmax, s_red[w]);
+        const double c = (double)cmax;
+        if (c > 0.0) atomicMax(&a.ctrl->smax_bits[0], (unsigned long long)__double_as_longlong(c));
+        if (any) atomicOr(&a.ctrl->flags, 1u);
+    }
+    if (D == 2) {
+        // last block of the step: Courant number and evolve_to_time rules
+        __shared__ int s_last;
+        if (threadIdx.x == 0) {
+            __threadfence();
+            s_last = atomicAdd(&a.ctrl->blocks_done, 1u) == gridDim.x - 1;
+        }
+        __syncthreads();
+        if (s_last && threadIdx.x == 0) {
+            __threadfence();
+            finish_step(a.ctrl, a.ctrl_mode, L.dt, 1.0, 1.0);
+        }
+    }
+}
+
+// The x-sweep (cells contiguous along the pencil) with the pencil across the
+// lanes of a warp instead: lane l holds cell c0 - 2 + l and the edge on its
+// left, neighbours come by shuffles, so every load is coalesced.  A window
+// updates the PLX = 28 cells c0 .. c0 + 27, and a warp takes NWX windows in
+// a row; the same arithmetic as k_pencil.
+constexpr int PLX = 28, NWX = 4;
+
+template <template <typename> class RPT, typename T>
+__global__ void __launch_bounds__(NT3) k_pencil_x(const Args3 a, const typename RPT<T>::Params P) {
+    using RP = RPT<T>;
+    constexpr int M = RP::M, MW = RP::MW, NR = RP::NR > 0 ? RP::NR : 1;
+    constexpr bool F64 = sizeof(T) == 8;
+    constexpr unsigned FULL = 0xffffffffu;
+    const Launch L = launch_state(a);
+    if (L.skip) return;
+    const double *__restrict__ qin = sweep_in(a, 0, L.par);
+    const double *src = a.split ? sweep_in(a, 0, L.par) : a.qin[L.par];
+    double *dst = sweep_out(a, 0, L.par);
+    const T dtdn = block_dtd<T>(L.dt, a.d[0]);
+    T cmax = (T)0;
+    bool bad = false;
+    const int lane = threadIdx.x & 31;
+    const long long win = ((long long)blockIdx.x * NT3 + threadIdx.x) >> 5;
+    if (win < a.npen) {  // whole warps: npen counts windows
+        const unsigned r = udiv((unsigned)win, a.pen0), ch = udiv(r, a.pen1);
+        const int y = (int)((unsigned)win - r * (unsigned)a.n[1]);
+        const int z = (int)(r - ch * (unsigned)a.n[2]);
+        const int n = a.n[0];
+        // NWX windows one after another (warp-uniform loop)
+#pragma unroll 1
+        for (int wi = 0; wi < NWX; wi++) {
+        const int c0 = ((int)ch * NWX + wi) * PLX;
+        if (c0 >= n) break;
+        const int x = c0 - 2 + lane;  // this lane's cell, and edge x on its left
+        const bool live = x <= n + 1;
+        T q[M], ql[M];
+        load_pencil<M, 0, T>(a, qin, min(x, n + 1), y, z, q);
+#pragma unroll
+        for (int k = 0; k < M; k++) ql[k] = __shfl_up_sync(FULL, q[k], 1);
+        T W[MW * M], sp[MW], am[M], ap[M], R[NR];
+        const bool eb = RP::template rpn3<0>(P, ql, q, W, sp, am, ap, R);
+        const bool edge = lane >= 1 && live;  // edges -1 .. n + 1
+        if (edge) {
+            bad |= eb;
+            if (x >= 0 && x <= n) {
+#pragma unroll
+                for (int qq = 0; qq < MW; qq++) {
+                    bad |= isnan_v(sp[qq]);
+                    cmax = max_abs(cmax, dtdn * sp[qq]);
+                }
+            }
+        }
+        // the upwind neighbour's unlimited wave of each family
+        T Wl[MW * M], Wr[MW * M];
+#pragma unroll
+        for (int qq = 0; qq < MW; qq++) {
+            const int from = gt0(sp[qq]) ? lane - 1 : lane + 1;
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                const T u = __shfl_sync(FULL, W[qq * M + k], from & 31);
+                Wl[qq * M + k] = u;
+                Wr[qq * M + k] = u;
+            }
+        }
+        T fa[M];
+        limit_edge<RP, T>(a, Wl, W, Wr, sp, dtdn, fa);
+        T amr[M], far[M];
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            amr[k] = __shfl_down_sync(FULL, am[k], 1);
+            far[k] = __shfl_down_sync(FULL, fa[k], 1);
+        }
+        if (lane >= 2 && lane < 2 + PLX && x < n) {
+            const size_t o = (size_t)M * ((size_t)x + (size_t)n * ((size_t)y + (size_t)a.n[1] * (size_t)z));
+            double q0[M];
+            load_cell<M>(src, o, q0);
+#pragma unroll
+            for (int k = 0; k < M; k++) {
+                const T qd = ((T)0 - dtdn * ap[k]) - dtdn * amr[k];
+                T v = F64 ? (T)q0[k] : (T)0;
+                v = (v + qd - dtdn * (far[k] - fa[k])) + (T)0;
+                q0[k] = F64 ? (double)v : q0[k] + f2d_bits((float)v);
+            }
+            store_cell<M>(dst, o, q0);
+        }
+        }
+    }
+    // block max and flag, then one atomic each
+    __shared__ T s_red[NT3 / 32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) cmax = tmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = cmax;
+    const int any = __syncthreads_or(bad ? 1 : 0);
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < NT3 / 32; w++) cmax = tmax(cmax, s_red[w]);
+        const double c = (double)cmax;
+        if (c > 0.0) atomicMax(&a.ctrl->smax_bits[0], (unsigned long long)__double_as_longlong(c));
+        if (any) atomicOr(&a.ctrl->flags, 1u);
+    }
+}
+
 template <template <typename> class RPT, int D, typename T>
 static int sweep(const gclaw3_solver *s, const Args3 &a, cudaStream_t st) {
     const typename RPT<T>::Params P = RPT<T>::make(s->problem_data);
     const unsigned nb = (unsigned)((a.npos + NT3 - 1) / NT3);
     const long long ncell = (long long)s->mx * s->my * s->mz;
     const unsigned nc = (unsigned)((ncell + NT3 - 1) / NT3);
-    k_edges<RPT, D, T><<<nb, NT3, 0, st>>>(a, P);
-    if (a.tw) {
-        k_chains<RPT, D, T, true><<<nb, NT3, 0, st>>>(a, P);
-        k_update<RPT, D, T, true><<<nc, NT3, 0, st>>>(a);
-    } else {
-        k_chains<RPT, D, T, false><<<nb, NT3, 0, st>>>(a, P);
-        k_update<RPT, D, T, false><<<nc, NT3, 0, st>>>(a);
+    if (!a.tw) {
+        // one kernel per sweep: warps across x for the x-sweep, threads
+        // marching along y or z (consecutive threads at consecutive x) else
+        constexpr int A0 = D == 0 ? 1 : 0, A1 = D == 2 ? 1 : 2;
+        Args3 b = a;
+        const int nn[3] = {s->mx, s->my, s->mz};
+        const int n0 = nn[A0], n1 = nn[A1], nd = nn[D];
+        b.pen0 = make_divisor(n0);
+        b.pen1 = make_divisor(n1);
+        if (D == 0) {
+            b.npen = (long long)n0 * n1 * ((nd + PLX * NWX - 1) / (PLX * NWX));
+            const unsigned np = (unsigned)((b.npen * 32 + NT3 - 1) / NT3);
+            k_pencil_x<RPT, T><<<np, NT3, 0, st>>>(b, P);
+        } else {
+            constexpr int PL = pencil_len<T>();
+            b.npen = (long long)n0 * n1 * ((nd + PL - 1) / PL);
+            const unsigned np = (unsigned)((b.npen + NT3 - 1) / NT3);
+            k_pencil<RPT, D == 0 ? 1 : D, T><<<np, NT3, 0, st>>>(b, P);
+        }
+        return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
     }
+    k_edges<RPT, D, T><<<nb, NT3, 0, st>>>(a, P);
+    k_chains<RPT, D, T><<<nb, NT3, 0, st>>>(a, P);
+    k_update<RPT, D, T><<<nc, NT3, 0, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
 }
 
@@ -745,6 +1122,10 @@ static int step_all(const gclaw3_solver *s, const Args3 &a, cudaStream_t st, int
     return s->precision == GCLAW_PREC_FP64 ? step_all_t<RPT, double>(s, a, st, nsteps)
                                            : step_all_t<RPT, float>(s, a, st, nsteps);
 }
+
+// state arrays start on 16 bytes (the pencil sweeps move cells of an even
+// number of components as double2)
+static bool al16(const void *p) { return ((size_t)p & 15u) == 0; }
 
 static long long box_positions(const gclaw3_solver *s) {
     return (long long)(s->mx + 3) * (long long)(s->my + 3) * (long long)(s->mz + 3);
@@ -831,7 +1212,8 @@ int gclaw3_step(const gclaw3_solver *s, const double *q_dev, double *qnew_dev, d
                 void *ws_dev, gclaw_ctrl *ctrl_dev, void *stream) {
     int rc = gclaw3_check(s);
     if (rc) return rc;
-    if (!q_dev || !qnew_dev || q_dev == qnew_dev || !ws_dev || !ctrl_dev || !(dt > 0.0))
+    if (!q_dev || !qnew_dev || q_dev == qnew_dev || !ws_dev || !ctrl_dev || !(dt > 0.0) ||
+        !al16(q_dev) || !al16(qnew_dev))
         return GCLAW_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(ctrl_dev, 0, sizeof(gclaw_ctrl), st) != cudaSuccess)
@@ -853,8 +1235,9 @@ int gclaw3_step_split(const gclaw3_solver *s, const double *q_dev, double *qnew_
                       void *stream) {
     int rc = gclaw3_check(s);
     if (rc) return rc;
-    if (!q_dev || !qnew_dev || !qtmp_dev || !ws_dev || !ctrl_dev || !(dt > 0.0) ||
-        q_dev == qnew_dev || qtmp_dev == q_dev || qtmp_dev == qnew_dev)
+    if (!q_dev || !qnew_dev || !qtmp_dev || !ctrl_dev || !(dt > 0.0) || q_dev == qnew_dev ||
+        qtmp_dev == q_dev || qtmp_dev == qnew_dev || !al16(q_dev) || !al16(qnew_dev) ||
+        !al16(qtmp_dev))
         return GCLAW_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(ctrl_dev, 0, sizeof(gclaw_ctrl), st) != cudaSuccess)
@@ -879,8 +1262,9 @@ int gclaw3_advance_split(const gclaw3_solver *s, double *q0_dev, double *q1_dev,
                          void *stream) {
     int rc = gclaw3_check(s);
     if (rc) return rc;
-    if (!q0_dev || !q1_dev || !qtmp_dev || !ws_dev || !ctrl_dev || nsteps < 0 ||
-        q0_dev == q1_dev || qtmp_dev == q0_dev || qtmp_dev == q1_dev)
+    if (!q0_dev || !q1_dev || !qtmp_dev || !ctrl_dev || nsteps < 0 || q0_dev == q1_dev ||
+        qtmp_dev == q0_dev || qtmp_dev == q1_dev || !al16(q0_dev) || !al16(q1_dev) ||
+        !al16(qtmp_dev))
         return GCLAW_ERR_ARG;
     Args3 a{};
     fill_args(s, a);
@@ -904,7 +1288,8 @@ int gclaw3_advance(const gclaw3_solver *s, double *q0_dev, double *q1_dev, void 
                    gclaw_ctrl *ctrl_dev, int nsteps, void *stream) {
     int rc = gclaw3_check(s);
     if (rc) return rc;
-    if (!q0_dev || !q1_dev || q0_dev == q1_dev || !ws_dev || !ctrl_dev || nsteps < 0)
+    if (!q0_dev || !q1_dev || q0_dev == q1_dev || !ws_dev || !ctrl_dev || nsteps < 0 ||
+        !al16(q0_dev) || !al16(q1_dev))
         return GCLAW_ERR_ARG;
     Args3 a{};
     fill_args(s, a);

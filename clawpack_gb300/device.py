@@ -200,7 +200,8 @@ class DeviceProblem3(DeviceProblem):
                   torch.empty(shape, dtype=torch.float64, device=self.device)]
         self.qtmp = (torch.empty(shape, dtype=torch.float64, device=self.device)
                      if self.split else None)
-        nbytes = L.gclaw3_workspace_bytes(ctypes.byref(self.s))
+        # split sweeps keep no edge records
+        nbytes = 0 if self.split else L.gclaw3_workspace_bytes(ctypes.byref(self.s))
         self.ws = torch.empty(int(nbytes), dtype=torch.uint8, device=self.device)
         self.ctrl = torch.zeros(256, dtype=torch.uint8, device=self.device)
         self._ctrl_host = torch.empty(256, dtype=torch.uint8, pin_memory=True)

@@ -55,6 +55,10 @@ int gclaw3_check(const gclaw3_solver *s);
 /* Bytes of device workspace a step of this grid needs. */
 size_t gclaw3_workspace_bytes(const gclaw3_solver *s);
 
+/* State arrays (q_dev, qnew_dev, q0_dev, q1_dev, qtmp_dev) start on a
+ * 16-byte boundary, as cudaMalloc returns them; others are refused with
+ * GCLAW_ERR_ARG. */
+
 /* One step of size dt from q_dev into qnew_dev (interior arrays, distinct).
  * ctrl_dev receives the Courant number (cfl) and status (GCLAW_OK or
  * GCLAW_NONPHYSICAL); only its reduction fields are used.  Asynchronous on
@@ -74,7 +78,8 @@ int gclaw3_advance(const gclaw3_solver *s, double *q0_dev, double *q1_dev, void 
  * z-sweeps in turn, each from the previous one's result with the boundary
  * conditions applied to it, without transverse terms (transverse_waves is
  * ignored); qtmp_dev is a third state buffer, distinct from the others.
- * The Courant number is the largest of the three sweeps'. */
+ * The Courant number is the largest of the three sweeps'.  Split sweeps
+ * keep no edge records: ws_dev is not used and may be NULL. */
 int gclaw3_step_split(const gclaw3_solver *s, const double *q_dev, double *qnew_dev,
                       double *qtmp_dev, double dt, void *ws_dev, gclaw_ctrl *ctrl_dev,
                       void *stream);

@@ -15,6 +15,7 @@ import math
 
 import numpy as np
 import pytest
+import torch
 
 from clawpack_gb300 import _lib
 from clawpack_gb300.device import DeviceProblem3, make_solver3_struct
@@ -311,6 +312,27 @@ def test_split_strict_bitwise(cuda, oracle, rp, shape, bcl, bcu):
     assert rel_l1(q32, qo) <= 2e-6 and abs(c32.cfl - cflo) <= 1e-6 * cflo
 
 
+@pytest.mark.parametrize("shape", [(130, 6, 5), (61, 34, 4), (5, 70, 3), (4, 3, 67)])
+@pytest.mark.parametrize("rp", [1, 2])
+def test_split_long_pencils(cuda, oracle, rp, shape):
+    """Pencils longer than a chunk (16 cells in FP32, 32 in FP64) and than
+    the x-sweep's warp windows (28 cells, four per warp)."""
+    rng = np.random.default_rng(sum(shape) + rp)
+    if rp == 1:
+        q, pd = np.asfortranarray(rng.normal(size=(4,) + shape)), PD3
+    else:
+        q, pd = euler3(shape, rng), [1.4]
+    d = (1.0 / shape[0], 1.0 / shape[1], 1.0 / shape[2])
+    dt = 0.04 * min(d)
+    bcl, bcu = [3, 2, 1], [1, 2, 3]
+    qo, cflo = oracle.step3_split(rp, pd, q, *d, dt, bcl, bcu, 2, [4] * 3, nthreads=4)
+    qs, c = gpu_split3(rp, pd, q, d, dt, bcl, bcu, strict=True)
+    assert np.array_equal(qs, qo), np.abs(qs - qo).max()
+    assert c.cfl == cflo
+    q32, c32 = gpu_split3(rp, pd, q, d, dt, bcl, bcu, precision=1)
+    assert rel_l1(q32, qo) <= 2e-6 and abs(c32.cfl - cflo) <= 1e-6 * cflo
+
+
 @pytest.mark.parametrize("order,lim", [(1, 0), (2, 1), (2, 0)])
 def test_split_options_strict_bitwise(cuda, oracle, order, lim):
     rng = np.random.default_rng(order * 10 + lim)
@@ -335,6 +357,20 @@ def test_split_refusals(cuda):
     assert L.gclaw3_step_split(sp, p[0], p[1], p[2], 0.0, ws, ctrl, None) == _lib.ERR_ARG
     assert L.gclaw3_advance_split(sp, p[0], p[1], p[1], ws, ctrl, 1, None) == _lib.ERR_ARG
     assert L.gclaw3_advance_split(sp, p[0], p[1], p[2], ws, ctrl, -1, None) == _lib.ERR_ARG
+    # state arrays off a 16-byte boundary are refused before any launch
+    off = ctypes.c_void_p(dev.q[1].data_ptr() + 8)
+    assert L.gclaw3_step_split(sp, p[0], off, p[2], 0.01, ws, ctrl, None) == _lib.ERR_ARG
+    assert L.gclaw3_advance_split(sp, off, p[0], p[2], ws, ctrl, 1, None) == _lib.ERR_ARG
+    big = torch.zeros(2 * dev.q[0].numel() + 2, dtype=torch.float64, device="cuda")
+    b0, b1 = (ctypes.c_void_p(big.data_ptr() + 8), ctypes.c_void_p(big.data_ptr() + 8 * (dev.q[0].numel() + 2)))
+    s.transverse_waves = 0
+    wsu = torch.empty(L.gclaw3_workspace_bytes(sp), dtype=torch.uint8, device="cuda")
+    assert L.gclaw3_step(sp, b0, b1, 0.01, ctypes.c_void_p(wsu.data_ptr()), ctrl, None) == _lib.ERR_ARG
+    assert L.gclaw3_advance(sp, b0, b1, ctypes.c_void_p(wsu.data_ptr()), ctrl, 1, None) == _lib.ERR_ARG
+    # split steps need no workspace
+    dev.upload(np.zeros((4, 8, 8, 8), order="F"))
+    assert L.gclaw3_step_split(sp, p[0], p[1], p[2], 0.01, None, ctrl, None) == 0
+    torch.cuda.synchronize()
 
 
 def test_split_clawsolver3d_run(cuda, oracle):
