@@ -224,3 +224,25 @@ def test_split_step_is_three_one_dimensional_sweeps():
     oute, _ = ref.step3_split(EU3, [1.4], e, 0.1, 0.1, 0.1, 0.004, [2] * 3, [2] * 3, 2, [4] * 3)
     for k in range(5):
         assert abs(oute[k].sum() - e[k].sum()) <= 1e-13 * np.abs(e[k]).sum()
+
+
+@pytest.mark.parametrize("order,lim", [(2, 4), (2, 1), (1, 0)])
+def test_z_uniform_split_is_the_2d_split_step(order, lim):
+    """On z-uniform data without z-velocity the z-sweep does nothing and the
+    x- and y-sweeps are those of the 2D split step (an independent
+    restatement, pinned by the 2D known answers)."""
+    rng = np.random.default_rng(70 + lim)
+    mx, my, mz = 14, 9, 4
+    q2 = rng.normal(size=(3, mx, my))
+    q3 = np.zeros((4, mx, my, mz), order="F")
+    q3[:3] = q2[..., None]
+    dx, dy, dz, dt = 0.1, 0.12, 0.5, 0.01
+    bcl, bcu = [1, 3], [3, 2]
+    out3, cfl3 = ref.step3_split(AC3, PD3, q3, dx, dy, dz, dt, bcl + [2], bcu + [2], order,
+                                 [lim, lim])
+    out2, cfl2, rc = ref.step_split(1, PD3, np.asfortranarray(q2), dx, dy, dt, bcl, bcu, order,
+                                    [lim, lim])
+    for l in range(mz):
+        assert rel_l1(out3[:3, :, :, l], out2) <= 1e-15
+    assert np.abs(out3[3]).max() == 0.0
+    assert cfl3 == pytest.approx(cfl2, rel=1e-15)
