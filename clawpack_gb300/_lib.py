@@ -147,6 +147,7 @@ SIGNATURES = {
     "gclaw_adjoint_step": (_I, [_SP, _P, _P, _P, _D, _P]),
     "gclaw_fp32_kernel": (_I, [_I]),
     "gclaw_fp64_kernel": (_I, [_I]),
+    "gclaw_split_kernel": (_I, [_I]),
     "gclaw_rcp_fp64": (_I, [_P, _P, ctypes.c_longlong, _P]),
     "gclaw_step_split": (_I, [_SP, _P, _P, _P, _D, _P, _P]),
     "gclaw_advance_split": (_I, [_SP, _P, _P, _P, _P, _I, _P]),

@@ -28,6 +28,7 @@
 #include <stdio.h>
 
 #include "gclaw.h"
+#include "gclaw_pencil2.cuh"
 #include "gclaw_step_impl.cuh"
 #include "gclaw_strip.cuh"
 
@@ -220,6 +221,9 @@ static int launch_tile(const gclaw_solver *s, const StepArgs &a, cudaStream_t st
 static int g_fp32_kernel = 0;
 // FP64 kernel family: 0 = default (tiles), 1 = tiles, 2 = strips.
 static int g_fp64_kernel = 0;
+// Split-step kernel family: 0 = default (pencil sweeps), 1 = tiles with a
+// sweep mask.
+static int g_split_kernel = 0;
 
 template <template <typename> class RPT, typename T>
 static int launch_strip(const gclaw_solver *s, const StepArgs &a, cudaStream_t st, int nlaunch) {
@@ -630,6 +634,12 @@ int gclaw_fp64_kernel(int which) {
     return prev;
 }
 
+int gclaw_split_kernel(int which) {
+    const int prev = g_split_kernel;
+    if (which >= 0 && which <= 1) g_split_kernel = which;
+    return prev;
+}
+
 int gclaw_step(const gclaw_solver *s, const double *q_dev, double *qnew_dev, double dt,
                gclaw_ctrl *ws_dev, void *stream) {
     int rc = gclaw_check(s);
@@ -664,9 +674,32 @@ int gclaw_advance(const gclaw_solver *s, double *q0_dev, double *q1_dev, gclaw_c
     return dispatch(s, a, (cudaStream_t)stream, nlaunch);
 }
 
+// state arrays of split steps start on 16 bytes (the pencil sweeps move
+// cells of an even number of components as double2)
+static bool al16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
 // Dimensionally split step: the x-sweep from qin into qtmp (its last block
 // keeps the CFL reduction open), then the y-sweep from qtmp into qout, whose
 // last block finishes the step with both sweeps' max |s|.
+// Pencil sweeps (gclaw_pencil2.cuh) by default, for the solvers without
+// aux; the tiles otherwise.
+static int split_pencils(const gclaw_solver *s, const StepArgs &ax, const StepArgs &ay,
+                         cudaStream_t st) {
+    const bool f64 = s->precision == GCLAW_PREC_FP64;
+    switch (s->rp) {
+    case GCLAW_RP_ACOUSTICS_2D:
+        return f64 ? p2::split_step<RpAcoustics, double>(s, ax, ay, st)
+                   : p2::split_step<RpAcoustics, float>(s, ax, ay, st);
+    case GCLAW_RP_SHALLOW_ROE_WITH_EFIX_2D:
+        return f64 ? p2::split_step<RpShallow, double>(s, ax, ay, st)
+                   : p2::split_step<RpShallow, float>(s, ax, ay, st);
+    case GCLAW_RP_EULER_4WAVE_2D:
+        return f64 ? p2::split_step<RpEuler, double>(s, ax, ay, st)
+                   : p2::split_step<RpEuler, float>(s, ax, ay, st);
+    default: return GCLAW_ERR_UNSUPPORTED;
+    }
+}
+
 static int dispatch_split(const gclaw_solver *s, StepArgs ax, cudaStream_t st, int nsteps,
                           double *qtmp) {
     StepArgs ay = ax;
@@ -679,8 +712,11 @@ static int dispatch_split(const gclaw_solver *s, StepArgs ax, cudaStream_t st, i
     ay.tw = 0;
     ay.qin[0] = ay.qin[1] = qtmp;
     for (int l = 0; l < nsteps; l++) {
-        int rc = dispatch(s, ax, st, 1);
-        if (rc == GCLAW_OK) rc = dispatch(s, ay, st, 1);
+        int rc = g_split_kernel == 0 ? split_pencils(s, ax, ay, st) : GCLAW_ERR_UNSUPPORTED;
+        if (rc == GCLAW_ERR_UNSUPPORTED) {
+            rc = dispatch(s, ax, st, 1);
+            if (rc == GCLAW_OK) rc = dispatch(s, ay, st, 1);
+        }
         if (rc != GCLAW_OK) return rc;
     }
     return GCLAW_OK;
@@ -693,6 +729,7 @@ int gclaw_step_split(const gclaw_solver *s, const double *q_dev, double *qnew_de
     if (!q_dev || !qnew_dev || !qtmp_dev || !ws_dev || !(dt > 0.0)) return GCLAW_ERR_ARG;
     if (rp_user_aux(s->rp) || s->capa) return GCLAW_ERR_UNSUPPORTED;
     if (qtmp_dev == q_dev || qtmp_dev == qnew_dev || q_dev == qnew_dev) return GCLAW_ERR_ARG;
+    if (!al16(q_dev) || !al16(qnew_dev) || !al16(qtmp_dev)) return GCLAW_ERR_ARG;
     StepArgs a{};
     fill_args(s, a);
     a.qin[0] = a.qin[1] = q_dev;
@@ -711,6 +748,7 @@ int gclaw_advance_split(const gclaw_solver *s, double *q0_dev, double *q1_dev, d
     if (!q0_dev || !q1_dev || !qtmp_dev || !ctrl_dev || nsteps < 0) return GCLAW_ERR_ARG;
     if (rp_user_aux(s->rp) || s->capa) return GCLAW_ERR_UNSUPPORTED;
     if (qtmp_dev == q0_dev || qtmp_dev == q1_dev || q0_dev == q1_dev) return GCLAW_ERR_ARG;
+    if (!al16(q0_dev) || !al16(q1_dev) || !al16(qtmp_dev)) return GCLAW_ERR_ARG;
     StepArgs a{};
     fill_args(s, a);
     a.qin[0] = q0_dev;

@@ -13,6 +13,24 @@
 
 namespace gclaw {
 
+// Division of a 32-bit index by a runtime divisor d >= 2 as a multiply-high
+// and a shift (Granlund and Montgomery, PLDI 1994): with l = ceil(log2 d)
+// and m = ceil(2^(31 + l) / d), which is below 2^32, floor(n / d) equals
+// umulhi(n, m) >> (l - 1) for every n < 2^31.
+struct Divisor {
+    unsigned m;
+    int s, d;
+};
+static Divisor make_divisor(int d) {
+    int l = 0;
+    while ((1ll << l) < d) l++;
+    const unsigned long long m = ((1ull << (31 + l)) + (unsigned long long)d - 1) / d;
+    return Divisor{(unsigned)m, l - 1, d};
+}
+__device__ __forceinline__ unsigned udiv(unsigned n, const Divisor &v) {
+    return __umulhi(n, v.m) >> v.s;
+}
+
 struct StepArgs {
     const double *qin[2];
     double *qout[2];

@@ -162,6 +162,12 @@ int gclaw_fp32_kernel(int which);
  * strips (bit-identical to tiles with -fmad=false). */
 int gclaw_fp64_kernel(int which);
 
+/* Kernel family of the dimensionally split step: 0 = default (one pencil
+ * kernel per sweep: warp windows along x, threads marching along y), 1 =
+ * the tile kernels with a sweep mask.  Both are bit-identical with
+ * -fmad=false.  Returns the previous setting. */
+int gclaw_split_kernel(int which);
+
 /* y[i] = 1 / x[i] with the reciprocal the product build uses for FP64
  * divisions (a Newton-Raphson iteration from an FP32 seed; IEEE division
  * for non-positive, denormal, infinite, NaN and very large x), n device
@@ -203,7 +209,10 @@ int gclaw_advance(const gclaw_solver *s, double *q0_dev, double *q1_dev, gclaw_c
  * of q_dev into qtmp_dev, then the y-sweep of qtmp_dev, with boundary
  * conditions applied to each input, into qnew_dev; no transverse waves.
  * The Courant number, the max of both sweeps', is left in ws_dev->cfl.
- * The three arrays are (num_eqn, mx, my) and distinct. */
+ * The three arrays are (num_eqn, mx, my), distinct, and start on a 16-byte
+ * boundary (as cudaMalloc returns them; others are refused with
+ * GCLAW_ERR_ARG).  Each sweep is one kernel over independent 1D problems
+ * (gclaw_split_kernel). */
 int gclaw_step_split(const gclaw_solver *s, const double *q_dev, double *qnew_dev,
                      double *qtmp_dev, double dt, gclaw_ctrl *ws_dev, void *stream);
 

@@ -18,7 +18,7 @@ from tests.helpers import PD, SHAPES, random_state, rel_l1
 
 pytestmark = pytest.mark.gpu
 
-SIZES = [(2, 2), (3, 70), (37, 29), (96, 40)]
+SIZES = [(2, 2), (3, 70), (37, 29), (96, 40), (250, 3), (131, 17)]
 BCS = [((1, 1), (1, 1)), ((2, 2), (2, 2)), ((3, 3), (3, 3)), ((3, 1), (1, 3))]
 
 
@@ -125,3 +125,25 @@ def test_default_solver_is_split_and_runs(cuda, oracle):
                                     cfl_max=w.cfl_max)
     assert rel_l1(outs[0], q) <= 1e-12
     assert pyclaw.ClawSolver2D(None).dimensional_split is True
+
+
+@pytest.mark.parametrize("rp", [1, 2, 3])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_pencil_and_tile_families_agree(cuda, rp, precision):
+    """The pencil sweeps (default) and the tile kernels with a sweep mask
+    (gclaw_split_kernel(1)) give bit-identical split steps in the strict
+    build, on a grid of several warp windows and column chunks."""
+    mx, my = 300, 77
+    rng = np.random.default_rng(rp + 10 * precision)
+    q = random_state(rp, mx, my, rng)
+    dx, dy = 1.0 / mx, 1.0 / my
+    s = split_struct(rp, mx, my, dx, dy, (3, 2), (1, 2), 4, precision=precision)
+    L = _lib.lib(True)
+    prev = L.gclaw_split_kernel(1)
+    try:
+        qt, ct = gpu_split_step(s, q, 0.04 * min(dx, dy), strict=True)
+    finally:
+        L.gclaw_split_kernel(prev)
+    qp, cp = gpu_split_step(s, q, 0.04 * min(dx, dy), strict=True)
+    assert np.array_equal(qt, qp)
+    assert ct.cfl == cp.cfl and ct.status == cp.status == 0
