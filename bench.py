@@ -206,10 +206,10 @@ def timed_steps(dev, steps, flush, torch):
     return ms * 1e-3, c1.numsteps - c0.numsteps, c1
 
 
-def run_variant(w, precision, steps, warmup, torch, flush, world, device):
+def run_variant(w, precision, steps, warmup, torch, flush, world, device, split=False):
     from clawpack_gb300.device import DeviceProblem
 
-    dev = DeviceProblem(w.solver_struct(precision), device=device)
+    dev = DeviceProblem(w.solver_struct(precision), device=device, split=split)
     dev.upload(w.q0)
     dev.ctrl_init(0.0, w.dt_initial, math.inf, cfl_max=w.cfl_max, cfl_desired=w.cfl_desired,
                   max_accepted=-1, max_steps=10 ** 9)
@@ -587,6 +587,23 @@ def run_ours(args):
                                          "traffic": None if t32 is None else round(t32 * cells)}}
         out["gpu_launches"] += args.steps
         del dev32
+        # ClawSolver2D's default: dimensionally split steps (x-sweep, boundary
+        # conditions, y-sweep), one pencil kernel per sweep; the state is read
+        # and written once per sweep: 2 x 2 x 24 B per cell-update
+        sp = {"workload": f"{w.name} {w.mx}x{w.my}, dimensionally split (ClawSolver2D "
+                          f"default), same step sequence rules",
+              "unit": UNIT, "alg_bytes_per_cell_update": 96}
+        for name, prec in (("fp64", 0), ("fp32_bulk", 1)):
+            ss, accs, cs, devs = run_variant(w, prec, args.steps, args.warmup, torch, flush, world,
+                                             device, split=True)
+            ach = 96 * cells / (ss / args.steps) * 1e-9
+            sp[name] = {"value": round(world * cells * accs / ss * 1e-9, 4),
+                        "ms_per_step": round(ss / args.steps * 1e3, 4),
+                        "roofline": {"bound": "hbm", "achieved": round(ach, 1), "peak": peak,
+                                     "unit": "GB/s", "frac": round(ach / peak, 4)}}
+            del devs
+        out["split"] = sp
+        out["gpu_launches"] += 4 * args.steps
     if not args.no_batched:
         out["batched"] = bench_batched(args, torch, world, device)
         out["gpu_launches"] += out["batched"]["launches"]
