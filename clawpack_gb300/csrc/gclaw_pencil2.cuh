@@ -6,16 +6,19 @@
 // A split sweep is a set of independent 1D problems along its axis, so one
 // kernel does the whole sweep with the state read once and written once and
 // no edge record in shared memory or HBM:
-//   p2_sweep_x  (x, cells contiguous along the pencil) a window of 32 cells
-//               across the lanes of a warp, lane l at cell c0 - 2 + l with
-//               the edge on its left; neighbours come by shuffles, every load
-//               is coalesced; a window updates 28 cells, a warp takes
-//               P2_NWX windows in a row;
+//   p2_sweep_w  a window of 32 cells along the sweep across the lanes of a
+//               warp, lane l at cell c0 - 2 + l with the edge on its left;
+//               neighbours come by shuffles; a window updates 28 cells, a
+//               warp takes P2_NWX windows in a row.  The x-sweep (cells
+//               contiguous, every load coalesced), and the y-sweep of
+//               euler_4wave_2D;
 //   p2_sweep_y  (y) each thread marches along a chunk of one column,
 //               consecutive threads at consecutive x, with the unlimited
 //               waves of three consecutive edges in registers: it solves the
 //               edge two ahead of the cell, limits the edge after it and
-//               updates the cell.
+//               updates the cell.  The y-sweep of the three-component
+//               solvers, whose windowed y-loads would touch twice the
+//               cache sectors.
 // The arithmetic and its order are those of step_kernel's phases with
 // transverse_waves 0 (phase_rpn2, phase_limit, phase_accum), so the
 // -fmad=false build stays bitwise equal to the oracle.  Columns and rows of
@@ -284,14 +287,17 @@ __device__ __forceinline__ void reduce2(const StepArgs &a, int slot, T smax, boo
     }
 }
 
-// ---- x-sweep: warp windows ------------------------------------------------
-template <template <typename> class RPT, typename T>
-__global__ void __launch_bounds__(NTP) p2_sweep_x(const StepArgs a, const typename RPT<T>::Params P,
-                                                  Divisor drow, long long nwarps) {
+// ---- warp windows along the sweep (x: rows; y: columns) --------------------
+// Warp w takes line w mod (lines) -- consecutive warps on neighbouring lines,
+// so that in the y-sweep the warps of a block share the cache sectors of
+// their rows -- and P2_NWX windows of that line in a row.
+template <template <typename> class RPT, typename T, int IXY>
+__global__ void __launch_bounds__(NTP) p2_sweep_w(const StepArgs a, const typename RPT<T>::Params P,
+                                                  Divisor dline, long long nwarps) {
     using RP = RPT<T>;
     constexpr int M = RP::M, MW = RP::MW, NA = RP::NA > 0 ? RP::NA : 1;
     constexpr unsigned FULL = 0xffffffffu;
-    const Launch2<T> L = launch2<T>(a, a.dx);
+    const Launch2<T> L = launch2<T>(a, IXY == 1 ? a.dx : a.dy);
     if (L.skip) return;
     const double *__restrict__ qin = L.par ? a.qin[1] : a.qin[0];
     double *qout = L.par ? a.qout[1] : a.qout[0];
@@ -301,16 +307,18 @@ __global__ void __launch_bounds__(NTP) p2_sweep_x(const StepArgs a, const typena
     const int lane = threadIdx.x & 31;
     const long long w = ((long long)blockIdx.x * NTP + threadIdx.x) >> 5;
     if (w < nwarps) {  // whole warps
-        const unsigned grp = udiv((unsigned)w, drow);
-        const int j = (int)((unsigned)w - grp * (unsigned)a.my);
-        const int n = a.mx;
+        const unsigned grp = udiv((unsigned)w, dline);
+        const int nl = IXY == 1 ? a.my : a.mx;  // lines across the sweep
+        const int line = (int)((unsigned)w - grp * (unsigned)nl);
+        const int n = IXY == 1 ? a.mx : a.my;
 #pragma unroll 1
         for (int wi = 0; wi < P2_NWX; wi++) {
             const int c0 = ((int)grp * P2_NWX + wi) * P2_WIN;
             if (c0 >= n) break;
             const int x = c0 - 2 + lane;  // this lane's cell, and edge x on its left
             T q[M], ql[M], aux[NA], al[NA];
-            load_cell2<M, 1, T>(a, qin, min(x, n + 1), j, q);
+            if (IXY == 1) load_cell2<M, 1, T>(a, qin, min(x, n + 1), line, q);
+            else load_cell2<M, 2, T>(a, qin, line, min(x, n + 1), q);
             if (RP::NA > 0) RP::cell_aux(P, q, aux);
 #pragma unroll
             for (int k = 0; k < M; k++) ql[k] = __shfl_up_sync(FULL, q[k], 1);
@@ -319,7 +327,7 @@ __global__ void __launch_bounds__(NTP) p2_sweep_x(const StepArgs a, const typena
             T W[MW * M], s[MW], am[M], ap[M];
             T sm = (T)0;
             bool bd = false;
-            solve2<RP, 1, T>(P, x, n, ql, al, q, aux, W, s, am, ap, sm, bd);
+            solve2<RP, IXY, T>(P, x, n, ql, al, q, aux, W, s, am, ap, sm, bd);
             if (lane >= 1 && x <= n + 1) {  // edges -1 .. n + 1
                 smax = tmax(smax, sm);
                 bad |= bd;
@@ -331,19 +339,20 @@ __global__ void __launch_bounds__(NTP) p2_sweep_x(const StepArgs a, const typena
                 const int from = (gt0(s[p]) ? lane - 1 : lane + 1) & 31;
 #pragma unroll
                 for (int k = 0; k < M; k++)
-                    Wn[p * M + k] = RP::template wnz<1>(p, k)
+                    Wn[p * M + k] = RP::template wnz<IXY>(p, k)
                                         ? __shfl_sync(FULL, W[p * M + k], from)
                                         : (T)0;
             }
             T fa[M], amr[M], far[M];
-            limit2<RP, 1, T>(a.mthlim, a.order, Wn, W, Wn, s, dtdn, fa);
+            limit2<RP, IXY, T>(a.mthlim, a.order, Wn, W, Wn, s, dtdn, fa);
 #pragma unroll
             for (int k = 0; k < M; k++) {
                 amr[k] = __shfl_down_sync(FULL, am[k], 1);
                 far[k] = __shfl_down_sync(FULL, fa[k], 1);
             }
             if (lane >= 2 && lane < 2 + P2_WIN && x < n) {
-                const size_t o = (size_t)M * ((size_t)x + (size_t)n * (size_t)j);
+                const size_t o = IXY == 1 ? (size_t)M * ((size_t)x + (size_t)a.mx * (size_t)line)
+                                          : (size_t)M * ((size_t)line + (size_t)a.mx * (size_t)x);
                 double q0[M];
                 load_row<M>(qin, o, q0);
                 update2<M, T>(q0, ap, amr, fa, far, dtdn);
@@ -351,7 +360,7 @@ __global__ void __launch_bounds__(NTP) p2_sweep_x(const StepArgs a, const typena
             }
         }
     }
-    reduce2<T>(a, 0, smax, bad, false, L.dt);
+    reduce2<T>(a, IXY - 1, smax, bad, IXY == 2 && !a.no_finish, L.dt);
 }
 
 // ---- y-sweep: marching columns ----------------------------------------------
@@ -435,16 +444,24 @@ __global__ void __launch_bounds__(NTP, ycol_blocks<RPT, T>())
 // thread numbering (the caller then runs the tile kernels).
 template <template <typename> class RPT, typename T>
 static int split_step(const gclaw_solver *s, const StepArgs &ax, const StepArgs &ay,
-                      cudaStream_t st) {
+                      cudaStream_t st, bool y_windows) {
     constexpr int PL = ycol_len<T>();
-    const long long nwarps = (long long)s->my * ((s->mx + P2_WIN * P2_NWX - 1) / (P2_WIN * P2_NWX));
+    constexpr int WW = P2_WIN * P2_NWX;
+    const long long nwarps = (long long)s->my * ((s->mx + WW - 1) / WW);
+    const long long nwarps_y = (long long)s->mx * ((s->my + WW - 1) / WW);
     const long long nthr = (long long)s->mx * ((s->my + PL - 1) / PL);
-    if (nwarps * 32 >= (1ll << 31) || nthr >= (1ll << 31)) return GCLAW_ERR_UNSUPPORTED;
+    if (nwarps * 32 >= (1ll << 31) || nwarps_y * 32 >= (1ll << 31) || nthr >= (1ll << 31))
+        return GCLAW_ERR_UNSUPPORTED;
     const typename RPT<T>::Params P = RPT<T>::make(s->problem_data);
     const unsigned bx = (unsigned)((nwarps * 32 + NTP - 1) / NTP);
-    const unsigned by = (unsigned)((nthr + NTP - 1) / NTP);
-    p2_sweep_x<RPT, T><<<bx, NTP, 0, st>>>(ax, P, make_divisor(s->my), nwarps);
-    p2_sweep_y<RPT, T><<<by, NTP, 0, st>>>(ay, P, make_divisor(s->mx), nthr);
+    p2_sweep_w<RPT, T, 1><<<bx, NTP, 0, st>>>(ax, P, make_divisor(s->my), nwarps);
+    if (y_windows) {
+        const unsigned by = (unsigned)((nwarps_y * 32 + NTP - 1) / NTP);
+        p2_sweep_w<RPT, T, 2><<<by, NTP, 0, st>>>(ay, P, make_divisor(s->mx), nwarps_y);
+    } else {
+        const unsigned by = (unsigned)((nthr + NTP - 1) / NTP);
+        p2_sweep_y<RPT, T><<<by, NTP, 0, st>>>(ay, P, make_divisor(s->mx), nthr);
+    }
     return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
 }
 

@@ -45,7 +45,7 @@ def main(argv=None):
     p.add_argument("--fp32-kernel", default="auto", choices=["auto", "tile", "strip"])
     p.add_argument("--fp64-kernel", default="auto", choices=["auto", "tile", "strip"])
     p.add_argument("--split", action="store_true", help="dimensionally split steps")
-    p.add_argument("--split-kernel", default="pencil", choices=["pencil", "tile"],
+    p.add_argument("--split-kernel", default="pencil", choices=["pencil", "tile", "march", "window"],
                    help="kernel family of 2D split steps")
     p.add_argument("--batched", type=int, default=0,
                    help="time the first N problems of the seeded shallow-water ensemble")
@@ -54,7 +54,7 @@ def main(argv=None):
 
     _lib.lib().gclaw_fp32_kernel({"auto": 0, "tile": 1, "strip": 2}[a.fp32_kernel])
     _lib.lib().gclaw_fp64_kernel({"auto": 0, "tile": 1, "strip": 2}[a.fp64_kernel])
-    _lib.lib().gclaw_split_kernel({"pencil": 0, "tile": 1}[a.split_kernel])
+    _lib.lib().gclaw_split_kernel({"pencil": 0, "tile": 1, "march": 2, "window": 3}[a.split_kernel])
     if a.batched:
         return run_batched(a)
     if a.workload in ("acoustics3d", "euler3d"):

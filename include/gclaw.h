@@ -163,8 +163,10 @@ int gclaw_fp32_kernel(int which);
 int gclaw_fp64_kernel(int which);
 
 /* Kernel family of the dimensionally split step: 0 = default (one pencil
- * kernel per sweep: warp windows along x, threads marching along y), 1 =
- * the tile kernels with a sweep mask.  Both are bit-identical with
+ * kernel per sweep: warp windows along x; along y threads marching up
+ * columns, or warp windows for euler_4wave_2D), 1 = the tile kernels with a
+ * sweep mask, 2 = pencils with marching columns for the y-sweep, 3 =
+ * pencils with warp windows for both sweeps.  All are bit-identical with
  * -fmad=false.  Returns the previous setting. */
 int gclaw_split_kernel(int which);
 

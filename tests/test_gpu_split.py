@@ -129,21 +129,25 @@ def test_default_solver_is_split_and_runs(cuda, oracle):
 
 @pytest.mark.parametrize("rp", [1, 2, 3])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_pencil_and_tile_families_agree(cuda, rp, precision):
-    """The pencil sweeps (default) and the tile kernels with a sweep mask
-    (gclaw_split_kernel(1)) give bit-identical split steps in the strict
-    build, on a grid of several warp windows and column chunks."""
-    mx, my = 300, 77
+def test_split_kernel_families_agree(cuda, rp, precision):
+    """The kernel families of the split step -- the default, the tile kernels
+    with a sweep mask (gclaw_split_kernel(1)), marching columns for the
+    y-sweep (2) and warp windows for both sweeps (3) -- give bit-identical
+    steps in the strict build, on a grid of several warp windows and column
+    chunks."""
+    mx, my = 300, 251
     rng = np.random.default_rng(rp + 10 * precision)
     q = random_state(rp, mx, my, rng)
     dx, dy = 1.0 / mx, 1.0 / my
     s = split_struct(rp, mx, my, dx, dy, (3, 2), (1, 2), 4, precision=precision)
     L = _lib.lib(True)
-    prev = L.gclaw_split_kernel(1)
-    try:
-        qt, ct = gpu_split_step(s, q, 0.04 * min(dx, dy), strict=True)
-    finally:
-        L.gclaw_split_kernel(prev)
-    qp, cp = gpu_split_step(s, q, 0.04 * min(dx, dy), strict=True)
-    assert np.array_equal(qt, qp)
-    assert ct.cfl == cp.cfl and ct.status == cp.status == 0
+    res = {}
+    for fam in (1, 2, 3, 0):
+        prev = L.gclaw_split_kernel(fam)
+        try:
+            res[fam] = gpu_split_step(s, q, 0.04 * min(dx, dy), strict=True)
+        finally:
+            L.gclaw_split_kernel(prev)
+    for fam in (1, 2, 3):
+        assert np.array_equal(res[fam][0], res[0][0]), fam
+        assert res[fam][1].cfl == res[0][1].cfl and res[fam][1].status == res[0][1].status == 0
