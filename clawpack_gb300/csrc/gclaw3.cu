@@ -953,91 +953,94 @@ __global__ void __launch_bounds__(NT3, pencil_blocks<RPT, T>()) k_pencil(const A
     }
 }
 
-// The x-sweep (cells contiguous along the pencil) with the pencil across the
-// lanes of a warp instead: lane l holds cell c0 - 2 + l and the edge on its
-// left, neighbours come by shuffles, so every load is coalesced.  A window
+// A sweep with the pencil across the lanes of a warp instead (the x-sweep,
+// whose cells are contiguous along the pencil; the y- and z-sweeps on
+// request): lane l holds cell c0 - 2 + l and the edge before it, and
+// neighbours come by shuffles; along x every load is coalesced, along y and
+// z consecutive warps take neighbouring lines (consecutive x).  A window
 // updates the PLX = 28 cells c0 .. c0 + 27, and a warp takes NWX windows in
 // a row; the same arithmetic as k_pencil.
 constexpr int PLX = 28, NWX = 4;
 
-template <template <typename> class RPT, typename T>
-__global__ void __launch_bounds__(NT3) k_pencil_x(const Args3 a, const typename RPT<T>::Params P) {
+template <template <typename> class RPT, int D, typename T>
+__global__ void __launch_bounds__(NT3) k_pencil_w(const Args3 a, const typename RPT<T>::Params P) {
     using RP = RPT<T>;
     constexpr int M = RP::M, MW = RP::MW, NR = RP::NR > 0 ? RP::NR : 1;
+    constexpr int A0 = D == 0 ? 1 : 0, A1 = D == 2 ? 1 : 2;
     constexpr bool F64 = sizeof(T) == 8;
     constexpr unsigned FULL = 0xffffffffu;
     const Launch L = launch_state(a);
     if (L.skip) return;
-    const double *__restrict__ qin = sweep_in(a, 0, L.par);
-    const double *src = a.split ? sweep_in(a, 0, L.par) : a.qin[L.par];
-    double *dst = sweep_out(a, 0, L.par);
-    const T dtdn = block_dtd<T>(L.dt, a.d[0]);
+    const double *__restrict__ qin = sweep_in(a, D, L.par);
+    const double *src = a.split ? sweep_in(a, D, L.par) : D == 0 ? a.qin[L.par] : a.qout[L.par];
+    double *dst = sweep_out(a, D, L.par);
+    const T dtdn = block_dtd<T>(L.dt, a.d[D]);
     T cmax = (T)0;
     bool bad = false;
     const int lane = threadIdx.x & 31;
     const long long win = ((long long)blockIdx.x * NT3 + threadIdx.x) >> 5;
-    if (win < a.npen) {  // whole warps: npen counts windows
+    if (win < a.npen) {  // whole warps: npen counts warps
+        int p[3];
         const unsigned r = udiv((unsigned)win, a.pen0), ch = udiv(r, a.pen1);
-        const int y = (int)((unsigned)win - r * (unsigned)a.n[1]);
-        const int z = (int)(r - ch * (unsigned)a.n[2]);
-        const int n = a.n[0];
+        p[A0] = (int)((unsigned)win - r * (unsigned)a.n[A0]);
+        p[A1] = (int)(r - ch * (unsigned)a.n[A1]);
+        const int n = a.n[D];
         // NWX windows one after another (warp-uniform loop)
 #pragma unroll 1
         for (int wi = 0; wi < NWX; wi++) {
-        const int c0 = ((int)ch * NWX + wi) * PLX;
-        if (c0 >= n) break;
-        const int x = c0 - 2 + lane;  // this lane's cell, and edge x on its left
-        const bool live = x <= n + 1;
-        T q[M], ql[M];
-        load_pencil<M, 0, T>(a, qin, min(x, n + 1), y, z, q);
+            const int c0 = ((int)ch * NWX + wi) * PLX;
+            if (c0 >= n) break;
+            const int x = c0 - 2 + lane;  // this lane's cell, and edge x before it
+            const bool live = x <= n + 1;
+            T q[M], ql[M];
+            p[D] = min(x, n + 1);
+            load_pencil<M, D, T>(a, qin, p[0], p[1], p[2], q);
 #pragma unroll
-        for (int k = 0; k < M; k++) ql[k] = __shfl_up_sync(FULL, q[k], 1);
-        T W[MW * M], sp[MW], am[M], ap[M], R[NR];
-        const bool eb = RP::template rpn3<0>(P, ql, q, W, sp, am, ap, R);
-        const bool edge = lane >= 1 && live;  // edges -1 .. n + 1
-        if (edge) {
-            bad |= eb;
-            if (x >= 0 && x <= n) {
+            for (int k = 0; k < M; k++) ql[k] = __shfl_up_sync(FULL, q[k], 1);
+            T W[MW * M], sp[MW], am[M], ap[M], R[NR];
+            const bool eb = RP::template rpn3<D>(P, ql, q, W, sp, am, ap, R);
+            if (lane >= 1 && live) {  // edges -1 .. n + 1
+                bad |= eb;
+                if (x >= 0 && x <= n) {
 #pragma unroll
-                for (int qq = 0; qq < MW; qq++) {
-                    bad |= isnan_v(sp[qq]);
-                    cmax = max_abs(cmax, dtdn * sp[qq]);
+                    for (int qq = 0; qq < MW; qq++) {
+                        bad |= isnan_v(sp[qq]);
+                        cmax = max_abs(cmax, dtdn * sp[qq]);
+                    }
                 }
             }
-        }
-        // the upwind neighbour's unlimited wave of each family
-        T Wl[MW * M], Wr[MW * M];
+            // the upwind neighbour's unlimited wave of each family
+            T Wl[MW * M];
 #pragma unroll
-        for (int qq = 0; qq < MW; qq++) {
-            const int from = gt0(sp[qq]) ? lane - 1 : lane + 1;
+            for (int qq = 0; qq < MW; qq++) {
+                const int from = gt0(sp[qq]) ? lane - 1 : lane + 1;
+#pragma unroll
+                for (int k = 0; k < M; k++)
+                    Wl[qq * M + k] = __shfl_sync(FULL, W[qq * M + k], from & 31);
+            }
+            T fa[M];
+            limit_edge<RP, T>(a, Wl, W, Wl, sp, dtdn, fa);
+            T amr[M], far[M];
 #pragma unroll
             for (int k = 0; k < M; k++) {
-                const T u = __shfl_sync(FULL, W[qq * M + k], from & 31);
-                Wl[qq * M + k] = u;
-                Wr[qq * M + k] = u;
+                amr[k] = __shfl_down_sync(FULL, am[k], 1);
+                far[k] = __shfl_down_sync(FULL, fa[k], 1);
             }
-        }
-        T fa[M];
-        limit_edge<RP, T>(a, Wl, W, Wr, sp, dtdn, fa);
-        T amr[M], far[M];
+            if (lane >= 2 && lane < 2 + PLX && x < n) {
+                p[D] = x;
+                const size_t o = (size_t)M * ((size_t)p[0] + (size_t)a.n[0] *
+                                              ((size_t)p[1] + (size_t)a.n[1] * (size_t)p[2]));
+                double q0[M];
+                load_cell<M>(src, o, q0);
 #pragma unroll
-        for (int k = 0; k < M; k++) {
-            amr[k] = __shfl_down_sync(FULL, am[k], 1);
-            far[k] = __shfl_down_sync(FULL, fa[k], 1);
-        }
-        if (lane >= 2 && lane < 2 + PLX && x < n) {
-            const size_t o = (size_t)M * ((size_t)x + (size_t)n * ((size_t)y + (size_t)a.n[1] * (size_t)z));
-            double q0[M];
-            load_cell<M>(src, o, q0);
-#pragma unroll
-            for (int k = 0; k < M; k++) {
-                const T qd = ((T)0 - dtdn * ap[k]) - dtdn * amr[k];
-                T v = F64 ? (T)q0[k] : (T)0;
-                v = (v + qd - dtdn * (far[k] - fa[k])) + (T)0;
-                q0[k] = F64 ? (double)v : q0[k] + f2d_bits((float)v);
+                for (int k = 0; k < M; k++) {
+                    const T qd = ((T)0 - dtdn * ap[k]) - dtdn * amr[k];
+                    T v = F64 ? (T)q0[k] : (T)0;
+                    v = (v + qd - dtdn * (far[k] - fa[k])) + (T)0;
+                    q0[k] = F64 ? (double)v : q0[k] + f2d_bits((float)v);
+                }
+                store_cell<M>(dst, o, q0);
             }
-            store_cell<M>(dst, o, q0);
-        }
         }
     }
     // block max and flag, then one atomic each
@@ -1052,7 +1055,24 @@ __global__ void __launch_bounds__(NT3) k_pencil_x(const Args3 a, const typename 
         if (c > 0.0) atomicMax(&a.ctrl->smax_bits[0], (unsigned long long)__double_as_longlong(c));
         if (any) atomicOr(&a.ctrl->flags, 1u);
     }
+    if (D == 2) {
+        // last block of the step: Courant number and evolve_to_time rules
+        __shared__ int s_last;
+        if (threadIdx.x == 0) {
+            __threadfence();
+            s_last = atomicAdd(&a.ctrl->blocks_done, 1u) == gridDim.x - 1;
+        }
+        __syncthreads();
+        if (s_last && threadIdx.x == 0) {
+            __threadfence();
+            finish_step(a.ctrl, a.ctrl_mode, L.dt, 1.0, 1.0);
+        }
+    }
 }
+
+// Kernel of the sweeps without transverse terms along y and z: 0 = default
+// (marching threads), 1 = marching threads, 2 = warp windows.
+static int g_pencil3 = 0;
 
 template <template <typename> class RPT, int D, typename T>
 static int sweep(const gclaw3_solver *s, const Args3 &a, cudaStream_t st) {
@@ -1069,10 +1089,15 @@ static int sweep(const gclaw3_solver *s, const Args3 &a, cudaStream_t st) {
         const int n0 = nn[A0], n1 = nn[A1], nd = nn[D];
         b.pen0 = make_divisor(n0);
         b.pen1 = make_divisor(n1);
-        if (D == 0) {
+        // windows along x; along y and z marching threads unless windows
+        // are asked for (measured slower for both solvers: euler_3D 128^3
+        // FP32 5.6 vs 8.6, acoustics_3D 192^3 FP32 12.3 vs 18.5
+        // Gcell-updates/s)
+        const bool win = D == 0 || g_pencil3 == 2;
+        if (win) {
             b.npen = (long long)n0 * n1 * ((nd + PLX * NWX - 1) / (PLX * NWX));
             const unsigned np = (unsigned)((b.npen * 32 + NT3 - 1) / NT3);
-            k_pencil_x<RPT, T><<<np, NT3, 0, st>>>(b, P);
+            k_pencil_w<RPT, D, T><<<np, NT3, 0, st>>>(b, P);
         } else {
             constexpr int PL = pencil_len<T>();
             b.npen = (long long)n0 * n1 * ((nd + PL - 1) / PL);
@@ -1142,6 +1167,12 @@ using namespace gclaw;
 using namespace gclaw::g3;
 
 extern "C" {
+
+int gclaw3_split_kernel(int which) {
+    const int prev = g_pencil3;
+    if (which >= 0 && which <= 2) g_pencil3 = which;
+    return prev;
+}
 
 int gclaw3_rp_shape(int rp, int *num_eqn, int *num_waves) {
     switch (rp) {

@@ -55,6 +55,7 @@ def main(argv=None):
     _lib.lib().gclaw_fp32_kernel({"auto": 0, "tile": 1, "strip": 2}[a.fp32_kernel])
     _lib.lib().gclaw_fp64_kernel({"auto": 0, "tile": 1, "strip": 2}[a.fp64_kernel])
     _lib.lib().gclaw_split_kernel({"pencil": 0, "tile": 1, "march": 2, "window": 3}[a.split_kernel])
+    _lib.lib().gclaw3_split_kernel({"pencil": 0, "tile": 0, "march": 1, "window": 2}[a.split_kernel])
     if a.batched:
         return run_batched(a)
     if a.workload in ("acoustics3d", "euler3d"):

@@ -87,6 +87,13 @@ int gclaw3_advance_split(const gclaw3_solver *s, double *q0_dev, double *q1_dev,
                          double *qtmp_dev, void *ws_dev, gclaw_ctrl *ctrl_dev, int nsteps,
                          void *stream);
 
+/* Kernel of the sweeps without transverse terms (split steps, and
+ * transverse_waves 0) along y and z: 0 = default (threads marching along
+ * the pencil), 1 = marching, 2 = warp windows across the pencil.  The
+ * x-sweep always runs on warp windows.  Bit-identical with -fmad=false.
+ * Returns the previous setting. */
+int gclaw3_split_kernel(int which);
+
 #ifdef __cplusplus
 }
 #endif

@@ -407,3 +407,31 @@ def test_split_clawsolver3d_run(cuda, oracle):
     for k in range(1, 4):
         q, t, dt, _ = oracle.evolve(step, q, t, 0.1 * k, dt, cfl_desired=0.9, cfl_max=1.0)
         assert rel_l1(claw.frames[k].q, q) <= 1e-12, k
+
+
+@pytest.mark.parametrize("rp", [1, 2])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_split_pencil_kernels_agree(cuda, rp, precision):
+    """Marching threads (gclaw3_split_kernel(1), the default) and warp
+    windows (2) along y and z give bit-identical split steps in the strict
+    build, on pencils longer than four windows."""
+    shape = (9, 130, 117)
+    rng = np.random.default_rng(rp + 3 * precision)
+    if rp == 1:
+        q, pd = np.asfortranarray(rng.normal(size=(4,) + shape)), PD3
+    else:
+        q, pd = euler3(shape, rng), [1.4]
+    d = (0.1, 1.0 / 130, 1.0 / 117)
+    dt = 0.04 * min(d)
+    L = _lib.lib(True)
+    res = {}
+    for fam in (1, 2, 0):
+        prev = L.gclaw3_split_kernel(fam)
+        try:
+            res[fam] = gpu_split3(rp, pd, q, d, dt, [3, 1, 2], [1, 3, 2], strict=True,
+                                  precision=precision)
+        finally:
+            L.gclaw3_split_kernel(prev)
+    for fam in (1, 2):
+        assert np.array_equal(res[fam][0], res[0][0]), fam
+        assert res[fam][1].cfl == res[0][1].cfl and res[fam][1].status == res[0][1].status == 0
