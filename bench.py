@@ -475,6 +475,21 @@ def bench_adjoint(torch, world, device):
             "launches": 2 * (2 * len(dts) + (len(dts) - nseg))}
 
 
+def cpu_model():
+    """The host CPU's model name as lscpu reports it (the machine type if
+    lscpu is missing)."""
+    import platform
+
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":", 1)[0].strip() == "Model name":
+                return f"{line.split(':', 1)[1].strip()} ({platform.machine()})"
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return platform.machine()
+
+
 def cpu_baseline(w, target_s=15.0):
     """The CPU oracle on the host cores (OpenMP, all threads) over a bounded
     number of full-grid steps."""
@@ -508,6 +523,7 @@ def cpu_baseline(w, target_s=15.0):
         n1 += 1
     secs1 = time.perf_counter() - t1
     return {"value": cells * n / secs * 1e-9, "unit": UNIT, "cores": threads, "kind": "port",
+            "cpu_model": cpu_model(),
             "sample": f"{n} full {w.mx}x{w.my} steps of the same problem on {threads} threads "
                       f"(OpenMP over slices), {secs:.1f} s",
             "one_thread": {"value": cells * n1 / secs1 * 1e-9, "cores": 1,
