@@ -700,7 +700,7 @@ def run_reference(args):
            "config": {"workload": f"shallow_dam_break {args.mx}x{args.mx} band sample",
                       "band_rows": band},
            "cpu_baseline": {"value": round(v, 5), "unit": UNIT, "cores": threads,
-                            "kind": "port", "sample": sample},
+                            "kind": "port", "cpu_model": cpu_model(), "sample": sample},
            "e2e": {"value": round(v, 5), "unit": UNIT, "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
