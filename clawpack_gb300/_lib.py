@@ -165,6 +165,7 @@ SIGNATURES = {
     "gclaw3_step_split": (_I, [_SP3, _P, _P, _P, _D, _P, _P, _P]),
     "gclaw3_advance_split": (_I, [_SP3, _P, _P, _P, _P, _P, _I, _P]),
     "gclaw3_split_kernel": (_I, [_I]),
+    "gclaw3_unsplit_kernel": (_I, [_I]),
 }
 
 _libs = {}

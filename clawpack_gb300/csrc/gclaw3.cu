@@ -391,6 +391,42 @@ __device__ __forceinline__ void load_cell(const double *src, size_t o, double *v
     }
 }
 
+// The M components of cell (g0, g1, g2), each coordinate in [-2, n+1],
+// through the boundary conditions of all three axes (load_q3's mapping, done
+// once per cell), converted to T.
+template <int M, typename T>
+__device__ __forceinline__ void load_cell3(const Args3 &a, const double *__restrict__ q, int g0,
+                                           int g1, int g2, T *out) {
+    int g[3] = {g0, g1, g2};
+    unsigned negm = 0u;  // components negated by walls
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int n = a.n[d];
+        int v = min(max(g[d], -2), n + 1);
+        if (v < 0) {
+            const int b = a.bc_lo[d];
+            if (b == GCLAW_BC_EXTRAP) v = 0;
+            else if (b == GCLAW_BC_PERIODIC) v = v + n;
+            else { v = -1 - v; negm |= 1u << (1 + d); }
+        } else if (v >= n) {
+            const int b = a.bc_hi[d];
+            if (b == GCLAW_BC_EXTRAP) v = n - 1;
+            else if (b == GCLAW_BC_PERIODIC) v = v - n;
+            else { v = 2 * n - 1 - v; negm |= 1u << (1 + d); }
+        }
+        g[d] = v;
+    }
+    const double *c = q + (size_t)M * ((size_t)g[0] + (size_t)a.n[0] *
+                                       ((size_t)g[1] + (size_t)a.n[1] * (size_t)g[2]));
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+        const double x = __ldg(c + k);
+        const bool neg = M > 1 && ((negm >> k) & 1u);
+        out[k] = from_double<T>(__longlong_as_double(__double_as_longlong(x) ^
+                                                     (neg ? (long long)0x8000000000000000ull : 0ll)));
+    }
+}
+
 // The state a sweep starts from and the one it writes.  Unsplit: every
 // sweep reads the old state, the x-sweep writes the new one and the others
 // add to it.  Split (x, y, z in turn): old -> new -> tmp -> new.
@@ -760,9 +796,9 @@ __global__ void __launch_bounds__(NT3) k_update(const Args3 a) {
 // Wc and speeds s, between the edges with waves Wl (before) and Wr (after)
 template <class RP, typename T>
 __device__ __forceinline__ void limit_edge(const Args3 &a, const T *Wl, const T *Wc, const T *Wr,
-                                           const T *s, T dtdn, T *fa) {
+                                           const T *s, T dtdn, T *fa, T *cq) {
     constexpr int M = RP::M, MW = RP::MW;
-    T W[MW * M], cq[M];
+    T W[MW * M];
 #pragma unroll
     for (int f = 0; f < MW * M; f++) W[f] = Wc[f];
 #pragma unroll
@@ -883,7 +919,7 @@ __global__ void __launch_bounds__(NT3, pencil_blocks<RPT, T>()) k_pencil(const A
         solve(c0, qb, qa, Wc, sc, am, apc);
         load(c0 + 1, qb);
         solve(c0 + 1, qa, qb, Wn, sn, amn, apn);
-        limit_edge<RP, T>(a, Wp, Wc, Wn, sc, dtdn, fa0);
+        { T cq_[RP::M]; limit_edge<RP, T>(a, Wp, Wc, Wn, sc, dtdn, fa0, cq_); }
         // qb holds the cell after the current one; the cell after that is
         // loaded an iteration ahead, so its latency overlaps the arithmetic
         T qf[M];
@@ -894,7 +930,7 @@ __global__ void __launch_bounds__(NT3, pencil_blocks<RPT, T>()) k_pencil(const A
             for (int k = 0; k < M; k++) qa[k] = qf[k];
             if (c + 1 < c1) load(c + 3, qf);
             solve(c + 2, qb, qa, Wx, sx, am, ap);
-            limit_edge<RP, T>(a, Wc, Wn, Wx, sn, dtdn, fa1);
+            { T cq_[RP::M]; limit_edge<RP, T>(a, Wc, Wn, Wx, sn, dtdn, fa1, cq_); }
             int g[3] = {p[0], p[1], p[2]};
             g[D] = c;
             const size_t o = (size_t)M * ((size_t)g[0] + (size_t)a.n[0] *
@@ -1019,7 +1055,7 @@ __global__ void __launch_bounds__(NT3) k_pencil_w(const Args3 a, const typename 
                     Wl[qq * M + k] = __shfl_sync(FULL, W[qq * M + k], from & 31);
             }
             T fa[M];
-            limit_edge<RP, T>(a, Wl, W, Wl, sp, dtdn, fa);
+            { T cq_[M]; limit_edge<RP, T>(a, Wl, W, Wl, sp, dtdn, fa, cq_); }
             T amr[M], far[M];
 #pragma unroll
             for (int k = 0; k < M; k++) {
@@ -1070,9 +1106,232 @@ __global__ void __launch_bounds__(NT3) k_pencil_w(const Args3 a, const typename 
     }
 }
 
+// ---- k_slab: a whole FP32-bulk sweep with transverse terms -----------------
+// The staged sweep (k_edges, k_chains, k_update) moves every edge record and
+// both transverse chains through HBM.  k_slab does the sweep in one kernel:
+// a block holds a tile of SA x SB pencils along the sweep (the interior
+// (SA-2) x (SB-2) and a one-pencil halo across it, SA along the axis that is
+// contiguous in memory where the sweep is not along x; SB per solver, see
+// slab_sb), one thread per pencil, marching together along a chunk of SL
+// cells.  Each thread keeps
+// the unlimited waves of three consecutive edges in registers (as k_pencil);
+// at cell c it solves edge c+2, limits edge c+1, runs the A-dQ chain of edge
+// c+1 into shared memory, and after a barrier the interior threads add to
+// cell c, in k_update's order, the first-order and correction terms of their
+// own pencil and the chain entries of the 3 x 3 pencils around (the A-dQ
+// chains of edge c+1, the A+dQ chains of edge c); after a second barrier
+// every thread stores the A+dQ chain of edge c+1 for the next cell.  The
+// arithmetic and its order are those of the staged kernels, so the strict
+// build stays bitwise equal to the oracle.  Halo pencils repeat their
+// neighbours' edges (the price of keeping the chains on chip), and pencils
+// in the ghost slices across the sweep take part exactly as the staged
+// kernels' box positions do.
+constexpr int SA = 32, SL = 16;
+// tile height: 8 (256 threads, 70 % of them on interior pencils); 16
+// (82 %, one 512-thread block per SM) measured slower for acoustics_3D at
+// 192^3 (4.16 against 4.41 Gcell-updates/s), and euler_3D's 60 chain slots
+// per buffer would not fit
+template <template <typename> class RPT>
+__host__ __device__ constexpr int slab_sb() {
+    return 8;
+}
+
+template <template <typename> class RPT, int D>
+__global__ void __launch_bounds__(SA * slab_sb<RPT>()) k_slab(const Args3 a,
+                                                               const typename RPT<float>::Params P) {
+    using T = float;
+    using RP = RPT<T>;
+    using F = Fields<RP>;
+    constexpr int SB = slab_sb<RPT>(), NTS = SA * SB;
+    constexpr int M = RP::M, MW = RP::MW, NR = RP::NR > 0 ? RP::NR : 1, NCH = F::NCH;
+    constexpr int T1 = (D + 1) % 3, T2 = (D + 2) % 3;
+    constexpr int TA = D == 0 ? 1 : 0;       // tile axis across threads (fastest)
+    constexpr int TB = 3 - D - TA;           // the other axis across the sweep
+    extern __shared__ __align__(16) unsigned char slab_smem[];
+    T *SAM = reinterpret_cast<T *>(slab_smem);  // A-dQ chains of edge c+1 [slot][thread]
+    T *SAP = SAM + NCH * NTS;                   // A+dQ chains of edge c [slot][thread]
+    const Launch L = launch_state(a);
+    if (L.skip) return;
+    __shared__ T s_dt[3];
+    if (threadIdx.x == 0) {
+        s_dt[0] = (T)(L.dt / a.d[D]);
+        s_dt[1] = (T)(L.dt / a.d[T1]);
+        s_dt[2] = (T)(L.dt / a.d[T2]);
+    }
+    __syncthreads();
+    const T dtdn = s_dt[0], dtt1 = s_dt[1], dtt2 = s_dt[2];
+    const double *__restrict__ qin = a.qin[L.par];
+    const double *src = D == 0 ? a.qin[L.par] : a.qout[L.par];
+    double *dst = a.qout[L.par];
+    const int tid = threadIdx.x, ta = tid % SA, tb = tid / SA;
+    int p[3];
+    p[TA] = (int)blockIdx.x * (SA - 2) - 1 + ta;
+    p[TB] = (int)blockIdx.y * (SB - 2) - 1 + tb;
+    const int n = a.n[D];
+    const int c0 = (int)blockIdx.z * SL, c1 = min(c0 + SL, n);
+    // slices -1..n across the sweep are edge positions of the staged box;
+    // threads past them (the ragged end of the last tiles) run along with
+    // clamped states and count nothing
+    const bool slice = p[TA] <= a.n[TA] && p[TB] <= a.n[TB];
+    const bool inner = ta >= 1 && ta <= SA - 2 && tb >= 1 && tb <= SB - 2 && p[TA] < a.n[TA] &&
+                       p[TB] < a.n[TB];
+    const int single = a.tw / 10;
+    const bool dbl = (a.tw % 10) > 0;
+    const T h = (T)0.5 * dtdn;
+    const T sixth = (T)(1.0 / 6.0);
+    const T f1 = sixth * dtdn * dtt1, f2 = sixth * dtdn * dtt2;
+    T cmax = (T)0;
+    bool bad = false;
+
+    auto load = [&](int c, T *q) {
+        int g[3] = {p[0], p[1], p[2]};
+        g[D] = c;
+        load_cell3<M, T>(a, qin, g[0], g[1], g[2], q);
+    };
+    auto solve = [&](int e, const T *ql, const T *qr, T *W, T *sp, T *amo, T *apo, T *R) {
+        const bool eb = RP::template rpn3<D>(P, ql, qr, W, sp, amo, apo, R);
+        if (slice) {
+            bad |= eb;
+            if (e >= 0 && e <= n) {
+#pragma unroll
+                for (int q = 0; q < MW; q++) {
+                    bad |= isnan_v(sp[q]);
+                    cmax = max_abs(cmax, dtdn * sp[q]);
+                }
+            }
+        }
+    };
+    // the fluctuation a chain splits: A-+dQ, with the correction flux folded
+    // in for transverse_waves 2x at second order
+    auto fold = [&](const T *x, const T *cq, T sign, T *out) {
+#pragma unroll
+        for (int k = 0; k < M; k++)
+            out[k] = (a.order == 2 && single == 2) ? (sign > (T)0 ? x[k] + cq[k] : x[k] - cq[k]) : x[k];
+    };
+
+    T qa[M], qb[M], qf[M], am[M], ap[M], Rx[NR], Rn[NR];
+    T Wp[MW * M], Wc[MW * M], Wn[MW * M], Wx[MW * M];
+    T sc[MW], sn[MW], sx[MW];
+    T apc[M], amn[M], apn[M], fa0[M], fa1[M], cq[M], asdq[M];
+    load(c0 - 2, qa);
+    load(c0 - 1, qb);
+    solve(c0 - 1, qa, qb, Wp, sx, am, ap, Rx);
+    load(c0, qa);
+    solve(c0, qb, qa, Wc, sc, am, apc, Rx);   // Rx: the state of edge c0
+    load(c0 + 1, qb);
+    solve(c0 + 1, qa, qb, Wn, sn, amn, apn, Rn);
+    limit_edge<RP, T>(a, Wp, Wc, Wn, sc, dtdn, fa0, cq);
+    // the A+dQ chain of edge c0
+    fold(apc, cq, (T)-1, asdq);
+    chain<RP, D, T>(P, Rx, asdq, dbl, h, f1, f2, SAP, NTS, tid, 0);
+    load(c0 + 2, qf);
+#pragma unroll 1
+    for (int c = c0; c < c1; c++) {
+#pragma unroll
+        for (int k = 0; k < M; k++) qa[k] = qf[k];
+        if (c + 1 < c1) load(c + 3, qf);
+        solve(c + 2, qb, qa, Wx, sx, am, ap, Rx);
+        limit_edge<RP, T>(a, Wc, Wn, Wx, sn, dtdn, fa1, cq);
+        // the A-dQ chain of edge c+1
+        fold(amn, cq, (T)1, asdq);
+        chain<RP, D, T>(P, Rn, asdq, dbl, h, f1, f2, SAM, NTS, tid, 0);
+        __syncthreads();
+        if (inner) {
+            int g[3] = {p[0], p[1], p[2]};
+            g[D] = c;
+            const size_t o = (size_t)M * ((size_t)g[0] + (size_t)a.n[0] *
+                                          ((size_t)g[1] + (size_t)a.n[1] * (size_t)g[2]));
+            T v[M];
+#pragma unroll
+            for (int k = 0; k < M; k++) v[k] = (T)0;
+#pragma unroll
+            for (int db = -1; db <= 1; db++)
+#pragma unroll
+                for (int da = -1; da <= 1; da++) {
+                    // pencil (T1 - da, T2 - db) of the tile
+                    const int nb = T1 == TA ? tid - da - SA * db : tid - db - SA * da;
+                    auto ent = [&](int part, int sd, int off, int k) -> T {
+                        const int slot = chain_slot<RP, D>(part, sd, off + 1, k);
+                        if (slot < 0) return ((T)0 + (T)0) + (T)0;
+                        return ((T)0 + SAM[slot * NTS + nb]) + SAP[slot * NTS + nb];
+                    };
+#pragma unroll
+                    for (int k = 0; k < M; k++) {
+                        if (da == 0 && db == 0) {
+                            const T qd = ((T)0 - dtdn * apc[k]) - dtdn * amn[k];
+                            v[k] = v[k] + qd - dtdn * (fa1[k] - fa0[k]) -
+                                   dtt1 * (ent(0, 1, 0, k) - ent(0, 0, 0, k)) -
+                                   dtt2 * (ent(1, 1, 0, k) - ent(1, 0, 0, k));
+                        } else {
+                            const T gt = da == 0 ? (T)0 - dtt1 * (ent(0, 1, db, k) - ent(0, 0, db, k))
+                                         : da == 1 ? dtt1 * ent(0, 1, db, k)
+                                                   : (T)0 - dtt1 * ent(0, 0, db, k);
+                            const T ht = db == 0 ? (T)0 - dtt2 * (ent(1, 1, da, k) - ent(1, 0, da, k))
+                                         : db == 1 ? dtt2 * ent(1, 1, da, k)
+                                                   : (T)0 - dtt2 * ent(1, 0, da, k);
+                            v[k] = v[k] + gt + ht;
+                        }
+                    }
+                }
+#pragma unroll
+            for (int k = 0; k < M; k++) dst[o + k] = src[o + k] + f2d_bits(v[k]);
+        }
+        __syncthreads();
+        // the A+dQ chain of edge c+1, for the next cell
+        fold(apn, cq, (T)-1, asdq);
+        chain<RP, D, T>(P, Rn, asdq, dbl, h, f1, f2, SAP, NTS, tid, 0);
+#pragma unroll
+        for (int f = 0; f < MW * M; f++) {
+            Wc[f] = Wn[f];
+            Wn[f] = Wx[f];
+        }
+#pragma unroll
+        for (int q = 0; q < MW; q++) sn[q] = sx[q];
+#pragma unroll
+        for (int k = 0; k < M; k++) {
+            apc[k] = apn[k];
+            amn[k] = am[k];
+            apn[k] = ap[k];
+            fa0[k] = fa1[k];
+            qb[k] = qa[k];
+        }
+#pragma unroll
+        for (int r = 0; r < NR; r++) Rn[r] = Rx[r];
+    }
+    // block max and flag, then one atomic each; the z-sweep's last block
+    // finishes the step
+    __shared__ T s_red[NTS / 32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) cmax = tmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, off));
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = cmax;
+    const int any = __syncthreads_or(bad ? 1 : 0);
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < NTS / 32; w++) cmax = tmax(cmax, s_red[w]);
+        const double cm = (double)cmax;
+        if (cm > 0.0) atomicMax(&a.ctrl->smax_bits[0], (unsigned long long)__double_as_longlong(cm));
+        if (any) atomicOr(&a.ctrl->flags, 1u);
+        if (D == 2) {
+            __threadfence();
+            const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
+            if (atomicAdd(&a.ctrl->blocks_done, 1u) == nblocks - 1) {
+                __threadfence();
+                finish_step(a.ctrl, a.ctrl_mode, L.dt, 1.0, 1.0);
+            }
+        }
+    }
+}
+
+template <template <typename> class RPT>
+constexpr size_t slab_smem() {
+    return sizeof(float) * 2 * (size_t)Fields<RPT<float>>::NCH * SA * slab_sb<RPT>();
+}
+
 // Kernel of the sweeps without transverse terms along y and z: 0 = default
 // (marching threads), 1 = marching threads, 2 = warp windows.
 static int g_pencil3 = 0;
+// Kernels of the sweeps with transverse terms: 0 = default (k_slab in
+// FP32-bulk, the staged kernels in FP64), 1 = the staged kernels.
+static int g_unsplit3 = 0;
 
 template <template <typename> class RPT, int D, typename T>
 static int sweep(const gclaw3_solver *s, const Args3 &a, cudaStream_t st) {
@@ -1105,6 +1364,27 @@ static int sweep(const gclaw3_solver *s, const Args3 &a, cudaStream_t st) {
             k_pencil<RPT, D == 0 ? 1 : D, T><<<np, NT3, 0, st>>>(b, P);
         }
         return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
+    }
+    if constexpr (sizeof(T) == 4) {
+        if (g_unsplit3 == 0) {
+            // FP32-bulk: the fused sweep (FP64 stays on the staged kernels,
+            // whose chains are bound by the FP64 pipe, where the halo
+            // pencils' repeated chains would cost more than the saved traffic)
+            constexpr int TA = D == 0 ? 1 : 0, TB = 3 - D - TA;
+            constexpr int SB = slab_sb<RPT>(), NTS = SA * SB;
+            const int nn[3] = {s->mx, s->my, s->mz};
+            const dim3 grid((unsigned)((nn[TA] + SA - 3) / (SA - 2)),
+                            (unsigned)((nn[TB] + SB - 3) / (SB - 2)),
+                            (unsigned)((nn[D] + SL - 1) / SL));
+            if (grid.y > 65535u || grid.z > 65535u) return GCLAW_ERR_ARG;
+            constexpr size_t sm = slab_smem<RPT>();
+            auto kern = k_slab<RPT, D>;
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
+                cudaSuccess)
+                return GCLAW_ERR_CUDA;
+            kern<<<grid, NTS, sm, st>>>(a, P);
+            return cudaGetLastError() == cudaSuccess ? GCLAW_OK : GCLAW_ERR_CUDA;
+        }
     }
     k_edges<RPT, D, T><<<nb, NT3, 0, st>>>(a, P);
     k_chains<RPT, D, T><<<nb, NT3, 0, st>>>(a, P);
@@ -1167,6 +1447,12 @@ using namespace gclaw;
 using namespace gclaw::g3;
 
 extern "C" {
+
+int gclaw3_unsplit_kernel(int which) {
+    const int prev = g_unsplit3;
+    if (which >= 0 && which <= 1) g_unsplit3 = which;
+    return prev;
+}
 
 int gclaw3_split_kernel(int which) {
     const int prev = g_pencil3;

@@ -94,6 +94,12 @@ int gclaw3_advance_split(const gclaw3_solver *s, double *q0_dev, double *q1_dev,
  * Returns the previous setting. */
 int gclaw3_split_kernel(int which);
 
+/* Kernels of the sweeps with transverse terms: 0 = default (FP32-bulk: one
+ * fused kernel per sweep, the chains exchanged in shared memory; FP64: the
+ * three staged kernels through the workspace), 1 = the staged kernels.
+ * Bit-identical with -fmad=false.  Returns the previous setting. */
+int gclaw3_unsplit_kernel(int which);
+
 #ifdef __cplusplus
 }
 #endif
