@@ -1136,8 +1136,15 @@ __host__ __device__ constexpr int slab_sb() {
     return 8;
 }
 
+// blocks per SM: three for acoustics_3D (57 KB of chain buffers each; the
+// kernel fits 80 registers without spilling), one for euler_3D (123 KB)
+template <template <typename> class RPT>
+constexpr int slab_blocks() {
+    return Fields<RPT<float>>::NCH <= 32 ? 3 : 1;
+}
+
 template <template <typename> class RPT, int D>
-__global__ void __launch_bounds__(SA * slab_sb<RPT>()) k_slab(const Args3 a,
+__global__ void __launch_bounds__(SA * slab_sb<RPT>(), slab_blocks<RPT>()) k_slab(const Args3 a,
                                                                const typename RPT<float>::Params P) {
     using T = float;
     using RP = RPT<T>;
