@@ -246,3 +246,28 @@ def test_z_uniform_split_is_the_2d_split_step(order, lim):
         assert rel_l1(out3[:3, :, :, l], out2) <= 1e-15
     assert np.abs(out3[3]).max() == 0.0
     assert cfl3 == pytest.approx(cfl2, rel=1e-15)
+
+
+def test_euler_z_uniform_first_order_split_is_the_2d_split_step():
+    """The split Euler step on z-uniform data without z-momentum, at first
+    order, equals the 2D split step of the 4-wave solver without entropy fix
+    (without limiting, grouping the entropy and shear waves changes
+    nothing); the z-sweep leaves the data as it is."""
+    rng = np.random.default_rng(77)
+    mx, my, mz = 14, 10, 4
+    q2 = euler_state((mx, my), rng)
+    q2[3] = 0.0
+    q2[4] = 1.5 / 0.4 + 0.5 * (q2[1] ** 2 + q2[2] ** 2) / q2[0]
+    q3 = np.zeros((5, mx, my, mz), order="F")
+    q3[0:3] = q2[0:3, ..., None]
+    q3[4] = q2[4, ..., None]
+    dx, dy, dz, dt = 0.1, 0.12, 0.5, 0.004
+    bcl, bcu = [1, 3], [3, 1]
+    out3, cfl3 = ref.step3_split(EU3, [1.4], q3, dx, dy, dz, dt, bcl + [2], bcu + [2], 1,
+                                 [0] * 3)
+    q24 = np.asfortranarray(q2[[0, 1, 2, 4]])
+    out2, cfl2, rc = ref.step_split(3, [1.4, 0.0], q24, dx, dy, dt, bcl, bcu, 1, [0] * 4)
+    assert rc == 0
+    for l in range(mz):
+        assert rel_l1(out3[[0, 1, 2, 4], :, :, l], out2) <= 1e-14
+    assert np.abs(out3[3]).max() <= 1e-14
