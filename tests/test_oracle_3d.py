@@ -271,3 +271,37 @@ def test_euler_z_uniform_first_order_split_is_the_2d_split_step():
     for l in range(mz):
         assert rel_l1(out3[[0, 1, 2, 4], :, :, l], out2) <= 1e-14
     assert np.abs(out3[3]).max() <= 1e-14
+
+
+def _plane_wave3(n, t):
+    """A pressure wave along (1, 1, 1) on the periodic unit cube: p =
+    sin(2 pi (x + y + z - sqrt(3) c t)), velocity p / Z along the
+    direction, exact for constant-coefficient acoustics."""
+    x = (np.arange(n) + 0.5) / n
+    X, Y, Z3 = np.meshgrid(x, x, x, indexing="ij")
+    c, Z = PD3[2], PD3[3]
+    f = np.sin(2 * np.pi * (X + Y + Z3) - 2 * np.pi * math.sqrt(3) * c * t)
+    q = np.zeros((4, n, n, n), order="F")
+    q[0] = f
+    q[1] = q[2] = q[3] = f / (Z * math.sqrt(3))
+    return q
+
+
+@pytest.mark.parametrize("tw", [22, 20])
+def test_unsplit_second_order_diagonal_wave(tw):
+    """Without limiting the unsplit 3D step converges at second order on a
+    smooth wave crossing the grid diagonally (the order the transverse and
+    corner terms exist for)."""
+    errs = []
+    T = 0.05
+    for n in (16, 32, 64):
+        q = _plane_wave3(n, 0.0)
+        dx = 1.0 / n
+        nsteps = int(round(T / (0.4 * dx / PD3[2])))
+        dt = T / nsteps
+        for _ in range(nsteps):
+            q, _ = ref.step3(AC3, PD3, q, dx, dx, dx, dt, [2] * 3, [2] * 3, 2, tw, [0, 0],
+                             nthreads=8)
+        errs.append(np.abs(q - _plane_wave3(n, T)).mean())
+    rates = [math.log2(errs[i] / errs[i + 1]) for i in range(2)]
+    assert min(rates) > 1.8, (errs, rates)
