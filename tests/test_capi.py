@@ -150,3 +150,49 @@ def test_fwave_solver_shape_and_checks():
     assert L.gclaw_check(ctypes.byref(s)) == 0
     s.problem_data[0] = 0.0  # gravity must be positive
     assert L.gclaw_check(ctypes.byref(s)) == _lib.ERR_ARG
+
+
+def test_split_and_3d_entry_points_refuse_unaligned_or_aliased_states():
+    """The split steps (2D and 3D) and the 3D steps move cells as 16-byte
+    vectors: state pointers off a 16-byte boundary, aliased state buffers
+    and bad step counts are refused before any CUDA call.  The pointer
+    values are never dereferenced."""
+    from clawpack_gb300.device import make_solver3_struct
+
+    L = _lib.lib()
+    P = ctypes.c_void_p
+    a, b, c, w = P(0x10000), P(0x20000), P(0x30000), P(0x40000)
+    off = P(0x30008)
+    s = good_solver()
+    assert L.gclaw_step_split(ctypes.byref(s), a, b, off, 0.1, w, None) == _lib.ERR_ARG
+    assert L.gclaw_step_split(ctypes.byref(s), a, b, a, 0.1, w, None) == _lib.ERR_ARG
+    assert L.gclaw_advance_split(ctypes.byref(s), P(0x10008), b, c, w, 1, None) == _lib.ERR_ARG
+    assert L.gclaw_advance_split(ctypes.byref(s), a, b, c, w, -1, None) == _lib.ERR_ARG
+    s3 = make_solver3_struct(1, 8, 8, 8, 0.1, 0.1, 0.1, [3] * 3, [3] * 3, [4, 4], 2, 22, 0,
+                             [1.0, 4.0, 2.0, 2.0])
+    r = ctypes.byref(s3)
+    assert L.gclaw3_step_split(r, a, b, off, 0.1, None, w, None) == _lib.ERR_ARG
+    assert L.gclaw3_step_split(r, a, b, b, 0.1, None, w, None) == _lib.ERR_ARG
+    assert L.gclaw3_step_split(r, a, b, c, 0.0, None, w, None) == _lib.ERR_ARG
+    assert L.gclaw3_advance_split(r, a, b, c, None, w, -1, None) == _lib.ERR_ARG
+    assert L.gclaw3_step(r, P(0x10008), b, 0.1, c, w, None) == _lib.ERR_ARG
+    assert L.gclaw3_advance(r, a, P(0x20008), c, w, 1, None) == _lib.ERR_ARG
+    s3.mx = 2000  # (mx + 3)(my + 3)(mz + 3) >= 2^31 once the others follow
+    s3.my = s3.mz = 1300
+    assert L.gclaw3_check(r) == _lib.ERR_ARG
+
+
+def test_kernel_family_switches():
+    """gclaw_split_kernel, gclaw3_split_kernel and gclaw3_unsplit_kernel
+    return the previous setting and ignore values out of range."""
+    L = _lib.lib()
+    for fn, top in ((L.gclaw_split_kernel, 3), (L.gclaw3_split_kernel, 2),
+                    (L.gclaw3_unsplit_kernel, 1)):
+        prev = fn(top)
+        try:
+            assert fn(top + 1) == top      # out of range: unchanged
+            assert fn(-1) == top
+            assert fn(0) == top
+            assert fn(0) == 0
+        finally:
+            fn(prev)
