@@ -4,7 +4,8 @@ upstream pyclaw/src/pyclaw/fileio/ascii.py (absent from the mounted tree).
 
 ``fort.qNNNN`` holds, per patch, the header of ``_header.patch_header``, a
 blank line, then one line per cell with its ``num_eqn`` values, cells in
-x-fastest order with a blank line after each row.  Values are written with
+x-fastest order with a blank line after each row (and, in 3D, after each
+z-slice).  Values are written with
 ``options['format']`` (default ``%18.8e``, Clawpack's ascii precision;
 ``%25.17e`` round-trips doubles exactly).
 """
@@ -21,16 +22,24 @@ DEFAULT_FORMAT = "%18.8e"
 
 
 def _cells_text(q, fmt):
-    """Text of the cell lines of one patch (q is (num_eqn, mx[, my]))."""
+    """Text of the cell lines of one patch (q is (num_eqn, mx[, my[, mz]])):
+    x fastest, a blank line after each row and, in 3D, another after each
+    z-slice."""
     m = q.shape[0]
     buf = io.StringIO()
     line = fmt * m
     if q.ndim == 2:
         np.savetxt(buf, q.T, fmt=line)
         buf.write("\n")
-    else:
+    elif q.ndim == 3:
         for j in range(q.shape[2]):
             np.savetxt(buf, q[:, :, j].T, fmt=line)
+            buf.write("\n")
+    else:
+        for k in range(q.shape[3]):
+            for j in range(q.shape[2]):
+                np.savetxt(buf, q[:, :, j, k].T, fmt=line)
+                buf.write("\n")
             buf.write("\n")
     return buf.getvalue()
 

@@ -1,7 +1,8 @@
 """Binary frames: the ascii headers (``fort.tNNNN`` with ``file_format
 binary64``, the patch header in ``fort.qNNNN``) and the cell values as
 little-endian float64 in ``fort.bNNNN``, in the order of the ascii values
-(component fastest, then x, then y; no ghost cells, ``num_ghost 0``)."""
+(component fastest, then x, then y, then z; no ghost cells, ``num_ghost
+0``)."""
 from __future__ import annotations
 
 import os

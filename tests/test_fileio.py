@@ -111,3 +111,38 @@ def test_controller_writes_every_frame(tmp_path):
         s = pyclaw.Solution(k, path=claw.outdir)
         assert abs(s.t - 0.25 * k) < 1e-12
         assert np.allclose(s.q, claw.frames[k].q, rtol=5e-9, atol=0)
+
+
+def small_solution3(mx, my, mz, t=0.25):
+    dims = [pyclaw.Dimension(-1.0, 1.0, n, name=c) for n, c in ((mx, "x"), (my, "y"), (mz, "z"))]
+    domain = pyclaw.Domain(dims)
+    state = pyclaw.State(domain, 4)
+    sol = pyclaw.Solution(state, domain)
+    sol.t = t
+    return sol
+
+
+@pytest.mark.parametrize("fmt", ["ascii", "binary"])
+def test_3d_round_trip(tmp_path, fmt):
+    """3D frames (ClawSolver3D's output): x fastest, then y, then z, with
+    the three dimensions in the patch header; exact at full precision."""
+    mx, my, mz = 7, 4, 3
+    sol = small_solution3(mx, my, mz, t=0.125)
+    sol.state.q = np.random.default_rng(5).normal(size=(4, mx, my, mz))
+    opts = {"format": "%25.17e"} if fmt == "ascii" else None
+    sol.write(3, str(tmp_path), file_format=fmt, options=opts)
+    assert " 3                 num_dim" in (tmp_path / "fort.t0003").read_text()
+    back = pyclaw.Solution(3, path=str(tmp_path), file_format=fmt)
+    assert back.q.shape == (4, mx, my, mz) and back.t == sol.t
+    assert np.array_equal(back.q, sol.q)
+    assert [d.num_cells for d in back.patch.dimensions] == [mx, my, mz]
+    assert [d.name for d in back.patch.dimensions] == ["x", "y", "z"]
+    if fmt == "ascii":
+        # the first value lines are the first row: q(:, i, 0, 0) for i = 0..mx-1
+        text = (tmp_path / "fort.q0003").read_text().split("\n\n", 1)[1]
+        rows = [ln for ln in text.splitlines() if ln.strip()]
+        assert len(rows) == mx * my * mz
+        first = np.array([[float(v) for v in ln.split()] for ln in rows[:mx]])
+        assert np.array_equal(first.T, sol.q[:, :, 0, 0])
+        second_slice = np.array([float(v) for v in rows[mx * my].split()])
+        assert np.array_equal(second_slice, sol.q[:, 0, 0, 1])
