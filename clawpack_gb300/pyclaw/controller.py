@@ -28,6 +28,9 @@ class Controller:
         self.outdir = "./_output"
         self.output_file_prefix = None
         self.output_options = {}
+        # aux arrays in the frame files: with frame 0 only, or with every frame
+        self.write_aux_init = False
+        self.write_aux_always = False
         self.frames = []
         self.logger = logging.getLogger("pyclaw.controller")
 
@@ -55,5 +58,6 @@ class Controller:
         if self.keep_copy:
             self.frames.append(self.solution.copy())
         if self.output_format is not None:
+            aux = self.write_aux_always or (self.write_aux_init and frame == 0)
             self.solution.write(frame, self.outdir, self.output_format, self.output_file_prefix,
-                                options=self.output_options)
+                                write_aux=aux, options=self.output_options)

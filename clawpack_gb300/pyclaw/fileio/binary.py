@@ -15,24 +15,31 @@ from .ascii import _install
 
 def write(solution, frame, path="./", file_prefix="fort", write_aux=False, options=None,
           write_p=False):
-    if write_aux or write_p:
-        raise NotImplementedError("aux and derived-quantity output are not supported")
+    """Write ``solution`` as frame ``frame`` under ``path``; with
+    ``write_aux`` the aux arrays too, as float64 in ``fort.aNNNN`` in the
+    order of ``fort.bNNNN``."""
+    if write_p:
+        raise NotImplementedError("derived-quantity output is not supported")
     file_prefix = file_prefix or "fort"
     os.makedirs(path, exist_ok=True)
     st = solution.state
     _header.write_t(path, file_prefix, frame, solution.t, st.num_eqn, len(solution.states),
-                    0, st.num_dim, 0, "binary64")
+                    getattr(st, "num_aux", 0), st.num_dim, 0, "binary64")
     with open(os.path.join(path, _header.frame_name(file_prefix, "q", frame)), "w") as f:
         for n, state in enumerate(solution.states, start=1):
             f.write(_header.patch_header(n, 1, state.patch))
     with open(os.path.join(path, _header.frame_name(file_prefix, "b", frame)), "wb") as f:
         for state in solution.states:
             np.asarray(state.q, dtype="<f8").ravel(order="F").tofile(f)
+    if write_aux and getattr(st, "num_aux", 0):
+        with open(os.path.join(path, _header.frame_name(file_prefix, "a", frame)), "wb") as f:
+            for state in solution.states:
+                np.asarray(state.aux, dtype="<f8").ravel(order="F").tofile(f)
 
 
 def read(solution, frame, path="./", file_prefix="fort", read_aux=False, options=None):
-    if read_aux:
-        raise NotImplementedError("aux arrays are not supported")
+    """Load frame ``frame`` into ``solution``; with ``read_aux`` the aux
+    arrays of ``fort.aNNNN`` too."""
     file_prefix = file_prefix or "fort"
     hdr = _header.read_t(path, file_prefix, frame)
     if hdr["num_ghost"] != 0:
@@ -51,4 +58,18 @@ def read(solution, frame, path="./", file_prefix="fort", read_aux=False, options
         q = data[off:off + count].reshape([hdr["num_eqn"]] + ncells, order="F")
         off += count
         patches.append((ncells, lower, delta, names, q.astype(np.float64)))
-    return _install(solution, hdr, patches)
+    aux = None
+    if read_aux:
+        if not hdr["num_aux"]:
+            raise ValueError("the frame's header lists no aux arrays")
+        adata = np.fromfile(os.path.join(path, _header.frame_name(file_prefix, "a", frame)),
+                            dtype="<f8")
+        aux, off = [], 0
+        for ncells, *_ in patches:
+            count = hdr["num_aux"] * int(np.prod(ncells))
+            if off + count > adata.size:
+                raise ValueError("binary aux file is shorter than its header")
+            aux.append(adata[off:off + count].reshape([hdr["num_aux"]] + list(ncells),
+                                                      order="F").astype(np.float64))
+            off += count
+    return _install(solution, hdr, patches, aux)

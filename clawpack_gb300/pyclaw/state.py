@@ -44,16 +44,16 @@ class State:
 
 class Solution:
     """``Solution(state, domain)``, or ``Solution(frame, path=..., file_format=...,
-    file_prefix=...)`` to load an output frame; ``solution.t`` is the time
-    of the state."""
+    file_prefix=..., read_aux=...)`` to load an output frame; ``solution.t``
+    is the time of the state."""
 
     def __init__(self, state, domain=None, path="./_output", file_format="ascii",
-                 file_prefix=None):
+                 file_prefix=None, read_aux=False):
         self.states = []
         self.domain = domain
         self.t = 0.0
         if isinstance(state, (int, np.integer)):
-            self.read(int(state), path, file_format, file_prefix)
+            self.read(int(state), path, file_format, file_prefix, read_aux)
         else:
             self.states = [state]
 

@@ -146,3 +146,52 @@ def test_3d_round_trip(tmp_path, fmt):
         assert np.array_equal(first.T, sol.q[:, :, 0, 0])
         second_slice = np.array([float(v) for v in rows[mx * my].split()])
         assert np.array_equal(second_slice, sol.q[:, 0, 0, 1])
+
+
+@pytest.mark.parametrize("fmt", ["ascii", "binary"])
+def test_aux_round_trip(tmp_path, fmt):
+    """Aux arrays (variable-coefficient and bathymetry solvers) go to
+    fort.aNNNN beside fort.qNNNN, num_aux in fort.tNNNN, and come back with
+    read_aux."""
+    mx, my = 9, 5
+    dims = [pyclaw.Dimension(0.0, 1.0, mx, name="x"), pyclaw.Dimension(0.0, 2.0, my, name="y")]
+    domain = pyclaw.Domain(dims)
+    state = pyclaw.State(domain, 3, 2)
+    rng = np.random.default_rng(9)
+    state.q = rng.normal(size=(3, mx, my))
+    state.aux = rng.random(size=(2, mx, my)) + 0.5
+    sol = pyclaw.Solution(state, domain)
+    opts = {"format": "%25.17e"} if fmt == "ascii" else None
+    sol.write(1, str(tmp_path), file_format=fmt, write_aux=True, options=opts)
+    assert "    2                 num_aux" in (tmp_path / "fort.t0001").read_text()
+    assert (tmp_path / "fort.a0001").exists()
+    back = pyclaw.Solution(1, path=str(tmp_path), file_format=fmt, read_aux=True)
+    assert np.array_equal(back.q, sol.q)
+    assert back.state.num_aux == 2 and np.array_equal(back.state.aux, state.aux)
+    # without read_aux the frame loads as before
+    assert pyclaw.Solution(1, path=str(tmp_path), file_format=fmt).state.aux is None
+    # a frame written without aux cannot be read with it
+    plain = pyclaw.Solution(pyclaw.State(domain, 3), domain)
+    plain.write(2, str(tmp_path), file_format=fmt)
+    with pytest.raises(ValueError):
+        pyclaw.Solution(2, path=str(tmp_path), file_format=fmt, read_aux=True)
+
+
+def test_controller_aux_output_options(tmp_path):
+    """write_aux_init writes the aux arrays with frame 0 only,
+    write_aux_always with every frame (PyClaw's Controller options)."""
+    dims = [pyclaw.Dimension(0.0, 1.0, 4, name="x"), pyclaw.Dimension(0.0, 1.0, 3, name="y")]
+    domain = pyclaw.Domain(dims)
+    state = pyclaw.State(domain, 3, 1)
+    state.aux = np.ones((1, 4, 3))
+    claw = pyclaw.Controller()
+    claw.solution = pyclaw.Solution(state, domain)
+    claw.output_format = "ascii"
+    for flag, sub in (("write_aux_init", "init"), ("write_aux_always", "always")):
+        claw.outdir = str(tmp_path / sub)
+        claw.write_aux_init = claw.write_aux_always = False
+        setattr(claw, flag, True)
+        claw._output(0)
+        claw._output(1)
+        has = [(tmp_path / sub / f"fort.a000{k}").exists() for k in (0, 1)]
+        assert has == ([True, False] if sub == "init" else [True, True])
